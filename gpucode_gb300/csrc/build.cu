@@ -1,0 +1,427 @@
+/*
+ * build.cu -- neighbour-list rebuild kernels (sm_103a).
+ *
+ * Replaces the reference's rebuild chain (ParticleSystem.cu:141-163):
+ * calcHashG -> thrust::sort_by_key -> reorderDataAndFindCellStartG ->
+ * NeighborFindG, plus CirWallListG and the history carry-over kernels.
+ *
+ * The cell sort is a stable counting sort over cells instead of a radix sort
+ * over hashes: (1) hash each particle and take an arrival rank in its cell with
+ * one atomic, (2) exclusive-scan the per-cell counts (three-phase, no
+ * inter-block waiting), which gives CellStart/CellEnd directly -- the
+ * reference's two 0xff memsets and the boundary kernel disappear, (3) scatter
+ * to sorted positions, (4) put each cell's few particles back into ascending
+ * particle-id order so ties come out exactly as thrust's stable sort leaves
+ * them.  The per-cell count lives in the CellEnd array until the scan
+ * overwrites it, so the only scratch is two ints per particle plus one per
+ * scan tile.
+ *
+ * The neighbour search keeps the reference's traversal order (level, z, y,
+ * x-row of cells, sorted order inside the row) so lists match it entry for
+ * entry, and evaluates the distance test in plain IEEE FP64 (this file is
+ * compiled with -fmad=false) so the integer output is bit-exact.
+ */
+#include <cuda_runtime.h>
+
+#include "dem_device.cuh"
+
+namespace dem {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanPerThread = 8;
+constexpr int kScanTile = kScanThreads * kScanPerThread; /* cells per scan tile */
+
+inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+/* (1) hash + arrival rank; count[] aliases cell_end[] and is zero on entry */
+__global__ void k_hash_count(const double3* __restrict__ pos, const int* __restrict__ plevel, int n,
+                             LevelView lv, double3 origin, int ncells, int* __restrict__ key,
+                             int* __restrict__ rank, int* __restrict__ count, int* __restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int lvl = plevel[i];
+  int h = grid_hash(grid_pos(pos[i], lvl, lv, origin), lvl, lv);
+  if (lvl != 0) h += lv.ncell_idx[lvl - 1];
+  /* the reference clamps to gridSize (not gridSize-1, kernel.cu:627-629), so a
+   * particle on the far face of the last level's grid hashes past the end; it
+   * would write out of bounds there.  Flag it and keep it in the last cell. */
+  if (h < 0 || h >= ncells) {
+    if (err) atomicOr(err, 4);
+    h = ncells - 1;
+  }
+  key[i] = h;
+  rank[i] = atomicAdd(&count[h], 1);
+}
+
+/* block-wide exclusive scan of one int per thread; returns the block total */
+__device__ __forceinline__ int block_exclusive_scan(int v, int& total) {
+  __shared__ int warp_tot[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int t = lane < kScanThreads / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < kScanThreads / 32) warp_tot[lane] = t;
+  }
+  __syncthreads();
+  const int warp_prefix = warp > 0 ? warp_tot[warp - 1] : 0;
+  total = warp_tot[kScanThreads / 32 - 1];
+  __syncthreads();
+  return warp_prefix + x - v;
+}
+
+/* (2a) per-tile totals */
+__global__ void k_tile_sums(const int* __restrict__ count, int ncells, int* __restrict__ tile_sum) {
+  const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanPerThread;
+  int s = 0;
+#pragma unroll
+  for (int e = 0; e < kScanPerThread; e++) {
+    long long c = base + e;
+    if (c < ncells) s += count[c];
+  }
+  int total;
+  block_exclusive_scan(s, total);
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+/* (2b) exclusive scan of the tile totals by one block (in place) */
+__global__ void k_scan_tiles(int* __restrict__ tile_sum, int ntiles) {
+  int carry = 0;
+  for (int base = 0; base < ntiles; base += kScanThreads) {
+    const int t = base + threadIdx.x;
+    const int v = t < ntiles ? tile_sum[t] : 0;
+    int total;
+    const int ex = block_exclusive_scan(v, total);
+    if (t < ntiles) tile_sum[t] = carry + ex;
+    carry += total;
+    __syncthreads();
+  }
+}
+
+/* (2c) cell offsets -> CellStart / CellEnd (-1 for empty cells); count[] is
+ * read from cell_end[] and overwritten in place */
+__global__ void k_cell_ranges(int* __restrict__ cell_start, int* __restrict__ cell_end, int ncells,
+                              const int* __restrict__ tile_off) {
+  const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanPerThread;
+  int c[kScanPerThread];
+  int s = 0;
+#pragma unroll
+  for (int e = 0; e < kScanPerThread; e++) {
+    long long q = base + e;
+    c[e] = q < ncells ? cell_end[q] : 0;
+    s += c[e];
+  }
+  int total;
+  int off = block_exclusive_scan(s, total) + tile_off[blockIdx.x];
+#pragma unroll
+  for (int e = 0; e < kScanPerThread; e++) {
+    long long q = base + e;
+    if (q < ncells) {
+      cell_start[q] = c[e] ? off : -1;
+      cell_end[q] = c[e] ? off + c[e] : -1;
+    }
+    off += c[e];
+  }
+}
+
+/* (3) scatter to sorted positions */
+__global__ void k_scatter(const int* __restrict__ key, const int* __restrict__ rank, int n,
+                          const int* __restrict__ cell_start, int* __restrict__ sorted_hash,
+                          int* __restrict__ sorted_src) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int h = key[i];
+  const int q = cell_start[h] + rank[i];
+  sorted_hash[q] = h;
+  sorted_src[q] = i;
+}
+
+/* (4) the first slot of each cell orders its cell by particle id (insertion
+ * sort; cells hold a handful of particles) */
+__global__ void k_cell_order(const int* __restrict__ sorted_hash, int* __restrict__ sorted_src,
+                             const int* __restrict__ cell_start, const int* __restrict__ cell_end,
+                             const int* __restrict__ order_key, int n) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int h = sorted_hash[q];
+  if (cell_start[h] != q) return;
+  const int e = cell_end[h];
+  for (int a = q + 1; a < e; a++) {
+    const int v = sorted_src[a];
+    const int kv = order_key ? order_key[v] : v;
+    int b = a - 1;
+    while (b >= q) {
+      const int u = sorted_src[b];
+      const int ku = order_key ? order_key[u] : u;
+      if (ku <= kv) break;
+      sorted_src[b + 1] = u;
+      b--;
+    }
+    sorted_src[b + 1] = v;
+  }
+}
+
+/* NeighborFindG (kernel.cu:729-855).  sorted_src == NULL means the particle
+ * arrays are themselves in sorted order. */
+__global__ void k_neighbor_find(const double3* __restrict__ pos, const double* __restrict__ rad,
+                                const int* __restrict__ sorted_src, const int* __restrict__ cell_start,
+                                const int* __restrict__ cell_end, const int* __restrict__ plevel,
+                                const int* __restrict__ nebor_idx, LevelView lv, double3 origin,
+                                double search_gap, int* __restrict__ nebor,
+                                int* __restrict__ num_nebor, int n, int* __restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double3 o = pos[i];
+  const double ri = rad[i];
+  const int L = plevel[i];
+  const long long base = slot_base(L, lv.level_npars, lv.level_nnebors) + nebor_idx[i];
+  const long long stride = lv.level_npars[L];
+  const int cap = lv.level_nnebors[L];
+  int count = 0;
+  bool over = false;
+  for (int iL = 0; iL < lv.n_levels; iL++) {
+    const int3 g = grid_pos(o, iL, lv, origin);
+    const int off = (int)ceil(lv.level_size[L] / lv.level_size[iL]);
+    const int cell_sum = iL != 0 ? lv.ncell_idx[iL - 1] : 0;
+    const int3 gs = lv.grid_size[iL];
+    for (int z = -off; z <= off; z++) {
+      for (int y = -off; y <= off; y++) {
+        int3 s = make_int3(g.x - off, g.y + y, g.z + z);
+        int3 e = make_int3(g.x + off, g.y + y, g.z + z);
+        if (s.x < 0) s.x = 0;
+        if (e.x > gs.x - 1) e.x = gs.x - 1;
+        if (s.y < 0 || s.z < 0 || s.y > gs.y - 1 || s.z > gs.z - 1) continue;
+        while (s.x != e.x) {
+          if (cell_start[grid_hash(s, iL, lv) + cell_sum] == -1) s.x++;
+          else break;
+        }
+        const int first = cell_start[grid_hash(s, iL, lv) + cell_sum];
+        while (s.x != e.x) {
+          if (cell_end[grid_hash(e, iL, lv) + cell_sum] == -1) e.x--;
+          else break;
+        }
+        const int last = cell_end[grid_hash(e, iL, lv) + cell_sum];
+        if (first == -1 || last == -1) continue;
+        for (int q = first; q < last; q++) {
+          const int j = sorted_src ? sorted_src[q] : q;
+          if (j == i) continue;
+          const double3 d = sub3(o, pos[j]);
+          if (len3(d) < rad[j] + ri + search_gap) {
+            if (count >= cap) {
+              over = true;
+              continue;
+            }
+            nebor[base + (long long)count * stride] = j;
+            count++;
+          }
+        }
+      }
+    }
+  }
+  num_nebor[i] = count;
+  if (over) atomicOr(err, 1);
+}
+
+/* CirWallListG (kernel.cu:1034-1073) */
+__global__ void k_wall_list(const double3* __restrict__ pos, const double* __restrict__ rad,
+                            const CylinderBC* __restrict__ cyl, int* __restrict__ wlist, size_t pitch,
+                            int* __restrict__ nwall, int n, double search_gap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double3 p = pos[i];
+  const double r = rad[i];
+  const CylinderBC c = *cyl;
+  int* row = (int*)((char*)wlist + (size_t)i * pitch);
+  int m = 0;
+  if (p.z >= (c.Tw - (2.0 * r + search_gap))) row[m++] = 0;
+  if (p.z <= ((2.0 * r + search_gap) + c.Bw)) row[m++] = 1;
+  const double dist = pow(pow((c.cir.x - p.x), 2.0) + pow((c.cir.y - p.y), 2.0), 0.5);
+  if (dist >= c.R - (2.0 * r + search_gap)) row[m++] = 2;
+  nwall[i] = m;
+}
+
+__device__ __forceinline__ void copy_slot(const HistSoA& dst, long long d, const HistSoA& src, long long s) {
+  dst.dispt[d] = src.dispt[s];
+  dst.nDsp[d] = src.nDsp[s];
+  dst.nDsp_mx[d] = src.nDsp_mx[s];
+  dst.plstRad[d] = src.plstRad[s];
+  dst.plstDfm[d] = src.plstDfm[s];
+  dst.stage[d] = src.stage[s];
+  dst.lqdBrg[d] = src.lqdBrg[s];
+}
+
+/* HstryCopyG (kernel.cu:869-911), with optional re-indexing of the old list */
+__global__ void k_carry_pp(const int* __restrict__ nebor, const int* __restrict__ nebor_old,
+                           const int* __restrict__ plevel, const int* __restrict__ nebor_idx,
+                           const int* __restrict__ nebor_idx_old, const int* __restrict__ level_npars,
+                           const int* __restrict__ level_nnebors, HistSoA old_h, HistSoA cur_h,
+                           const int* __restrict__ num_nebor, const int* __restrict__ num_nebor_old,
+                           const int* __restrict__ old_src, const int* __restrict__ old_to_new, int n) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int p = old_src ? old_src[q] : q;
+  const int L = plevel[q];
+  const long long stride = level_npars[L];
+  const long long lb = slot_base(L, level_npars, level_nnebors);
+  const long long nb = lb + nebor_idx[q];
+  const long long ob = lb + nebor_idx_old[p];
+  const int nn = num_nebor[q], no = num_nebor_old[p];
+  for (int a = 0; a < nn; a++) {
+    const long long ine = nb + a * stride;
+    const int partner = nebor[ine];
+    for (int b = 0; b < no; b++) {
+      const long long jne = ob + b * stride;
+      int j = nebor_old[jne];
+      if (old_to_new) j = old_to_new[j];
+      if (j == partner) copy_slot(cur_h, ine, old_h, jne);
+    }
+  }
+}
+
+/* HstryCopyPWG (kernel.cu:918-950) */
+__global__ void k_carry_pw(const int* __restrict__ wlist, size_t pitch, const int* __restrict__ wlist_old,
+                           size_t pitch_old, HistSoA old_h, HistSoA cur_h, const int* __restrict__ nwall,
+                           const int* __restrict__ nwall_old, const int* __restrict__ old_src, int n,
+                           int np_new, int np_old) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int p = old_src ? old_src[q] : q;
+  const int* row = (const int*)((const char*)wlist + (size_t)q * pitch);
+  const int* orow = (const int*)((const char*)wlist_old + (size_t)p * pitch_old);
+  for (int a = 0; a < nwall[q]; a++) {
+    const int w = row[a];
+    for (int b = 0; b < nwall_old[p]; b++)
+      if (orow[b] == w) copy_slot(cur_h, (long long)a * np_new + q, old_h, (long long)b * np_old + p);
+  }
+}
+
+/* old <- cur, cur <- 0 over count slots (PPCntHstryCopy / WallCntHstryCopy) */
+__global__ void k_rotate(HistSoA old_h, HistSoA cur_h, long long count) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    old_h.dispt[i] = cur_h.dispt[i];
+    old_h.nDsp[i] = cur_h.nDsp[i];
+    old_h.nDsp_mx[i] = cur_h.nDsp_mx[i];
+    old_h.plstRad[i] = cur_h.plstRad[i];
+    old_h.plstDfm[i] = cur_h.plstDfm[i];
+    old_h.stage[i] = cur_h.stage[i];
+    old_h.lqdBrg[i] = cur_h.lqdBrg[i];
+    cur_h.dispt[i] = make_double3(0.0, 0.0, 0.0);
+    cur_h.nDsp[i] = 0.0;
+    cur_h.nDsp_mx[i] = 0.0;
+    cur_h.plstRad[i] = 0.0;
+    cur_h.plstDfm[i] = 0.0;
+    cur_h.stage[i] = 0;
+    cur_h.lqdBrg[i] = 0;
+  }
+}
+
+__global__ void k_scan_small(const int* __restrict__ in, int* __restrict__ out, int n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int acc = 0;
+    for (int i = 0; i < n; i++) {
+      acc += in[i];
+      out[i] = acc;
+    }
+  }
+}
+
+int grid_for(long long n, int block) { return n <= 0 ? 1 : div_up(n, block); }
+
+}  // namespace
+
+size_t sort_scratch_bytes(int np, int ncells) {
+  const size_t tiles = (size_t)div_up(ncells, kScanTile);
+  return sizeof(int) * (2 * (size_t)np + tiles + 64);
+}
+
+dem_status cell_sort(const double3* pos, const int* plevel, const int* order_key, int n, LevelView lv,
+                     const DevConsts& k, int ncells, int* sorted_hash, int* sorted_src, int* cell_start,
+                     int* cell_end, void* scratch, int* err, cudaStream_t stream) {
+  if (n < 0 || ncells <= 0) return fail(DEM_ERR_ARG, "cell_sort: bad sizes");
+  int* key = (int*)scratch;
+  int* rank = key + n;
+  int* tile = rank + n;
+  const int ntiles = div_up(ncells, kScanTile);
+  cudaError_t e = cudaMemsetAsync(cell_end, 0, sizeof(int) * (size_t)ncells, stream);
+  if (e != cudaSuccess) return cuda_check(e, "cell_sort memset");
+  if (n > 0)
+    k_hash_count<<<grid_for(n, 256), 256, 0, stream>>>(pos, plevel, n, lv, k.prm.Origin, ncells, key, rank,
+                                                      cell_end, err);
+  k_tile_sums<<<ntiles, kScanThreads, 0, stream>>>(cell_end, ncells, tile);
+  k_scan_tiles<<<1, kScanThreads, 0, stream>>>(tile, ntiles);
+  k_cell_ranges<<<ntiles, kScanThreads, 0, stream>>>(cell_start, cell_end, ncells, tile);
+  if (n > 0) {
+    k_scatter<<<grid_for(n, 256), 256, 0, stream>>>(key, rank, n, cell_start, sorted_hash, sorted_src);
+    k_cell_order<<<grid_for(n, 256), 256, 0, stream>>>(sorted_hash, sorted_src, cell_start, cell_end,
+                                                      order_key, n);
+  }
+  return cuda_check(cudaGetLastError(), "cell_sort launch");
+}
+
+dem_status neighbor_find(const double3* pos, const double* rad, const int* sorted_src,
+                         const int* cell_start, const int* cell_end, const int* plevel, const int* nebor_idx,
+                         LevelView lv, const DevConsts& k, int* nebor, int* num_nebor, int n, int* err,
+                         cudaStream_t stream) {
+  if (n <= 0) return DEM_OK;
+  k_neighbor_find<<<grid_for(n, 128), 128, 0, stream>>>(pos, rad, sorted_src, cell_start, cell_end, plevel,
+                                                       nebor_idx, lv, k.prm.Origin, k.prm.SearchGap, nebor,
+                                                       num_nebor, n, err);
+  return cuda_check(cudaGetLastError(), "neighbor_find launch");
+}
+
+dem_status wall_list(const double3* pos, const double* rad, const CylinderBC* cyl, int* wlist, size_t pitch,
+                     int* nwall, int n, const DevConsts& k, cudaStream_t stream) {
+  if (n <= 0) return DEM_OK;
+  k_wall_list<<<grid_for(n, 128), 128, 0, stream>>>(pos, rad, cyl, wlist, pitch, nwall, n, k.prm.SearchGap);
+  return cuda_check(cudaGetLastError(), "wall_list launch");
+}
+
+dem_status history_carry_pp(const int* nebor, const int* nebor_old, const int* plevel, const int* nebor_idx,
+                            const int* nebor_idx_old, const int* level_npars, const int* level_nnebors,
+                            HistSoA old_h, HistSoA cur_h, const int* num_nebor, const int* num_nebor_old,
+                            const int* old_src, const int* old_to_new, int n, cudaStream_t stream) {
+  if (n <= 0) return DEM_OK;
+  k_carry_pp<<<grid_for(n, 256), 256, 0, stream>>>(nebor, nebor_old, plevel, nebor_idx, nebor_idx_old,
+                                                  level_npars, level_nnebors, old_h, cur_h, num_nebor,
+                                                  num_nebor_old, old_src, old_to_new, n);
+  return cuda_check(cudaGetLastError(), "history_carry_pp launch");
+}
+
+dem_status history_carry_pw(const int* wlist, size_t pitch, const int* wlist_old, size_t pitch_old,
+                            HistSoA old_h, HistSoA cur_h, const int* nwall, const int* nwall_old,
+                            const int* old_src, int n, int np_new, int np_old, cudaStream_t stream) {
+  if (n <= 0) return DEM_OK;
+  k_carry_pw<<<grid_for(n, 128), 128, 0, stream>>>(wlist, pitch, wlist_old, pitch_old, old_h, cur_h, nwall,
+                                                  nwall_old, old_src, n, np_new, np_old);
+  return cuda_check(cudaGetLastError(), "history_carry_pw launch");
+}
+
+dem_status history_rotate(HistSoA old_h, HistSoA cur_h, long long count, cudaStream_t stream) {
+  if (count <= 0) return DEM_OK;
+  long long blocks = (count + 255) / 256;
+  if (blocks > 152LL * 16) blocks = 152LL * 16;
+  k_rotate<<<(int)blocks, 256, 0, stream>>>(old_h, cur_h, count);
+  return cuda_check(cudaGetLastError(), "history_rotate launch");
+}
+
+dem_status inclusive_scan_small(const int* in, int* out, int n, cudaStream_t stream) {
+  if (n <= 0) return DEM_OK;
+  k_scan_small<<<1, 32, 0, stream>>>(in, out, n);
+  return cuda_check(cudaGetLastError(), "scan launch");
+}
+
+}  // namespace dem

@@ -1,0 +1,810 @@
+/*
+ * engine.cu -- the native DEM engine (dem_* API) on one GB300.
+ *
+ * One time step is the reference's main.cpp:466-564 sequence -- rebuild when
+ * the last integration flagged it, then p-p forces, wall forces, integration
+ * -- with three GB300-specific changes:
+ *  - the rebuild decision is taken on the device: each step starts with a
+ *    one-thread kernel that reads the rebuild flag and sets the condition of a
+ *    CUDA-graph IF node whose body is the whole rebuild, so a graph of many
+ *    steps replays with no host round trip (the reference copies the flag to
+ *    the host every step, main.cpp:470);
+ *  - particles are kept in cell order: every rebuild permutes the particle
+ *    state by the cell sort, so neighbours of consecutive particles are close
+ *    in memory, and neighbour slots of consecutive particles are adjacent;
+ *  - contact history is 64-byte records (one per slot) instead of seven
+ *    parallel arrays; a rebuild copies only the used slots to the *_old
+ *    buffers and the carry-over writes every used new slot (match -> copy,
+ *    else zero), replacing the reference's full-array copy + memset
+ *    (ParticleSystem.cu:336-375).
+ *
+ * Precision: DEM_PREC_FP64 runs the reference formulas (step64.cu) on these
+ * buffers; DEM_PREC_MIXED runs the fused FP32-force / FP64-state kernel of
+ * mixed.cu.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dem_device.cuh"
+#include "engine.h"
+
+namespace dem {
+namespace {
+
+inline int grid_for(long long n, int block) { return n <= 0 ? 1 : (int)((n + block - 1) / block); }
+
+template <class T>
+dem_status dalloc(dem_ctx* c, T** p, size_t count) {
+  void* q = nullptr;
+  dem_status st = cuda_alloc(&q, sizeof(T) * (count ? count : 1));
+  if (st != DEM_OK) return st;
+  cudaError_t e = cudaMemset(q, 0, sizeof(T) * (count ? count : 1));
+  if (e != cudaSuccess) {
+    cudaFree(q);
+    return cuda_check(e, "cudaMemset");
+  }
+  c->allocs.push_back(q);
+  *p = (T*)q;
+  return DEM_OK;
+}
+
+__global__ void k_zero_int(int* p, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = 0;
+}
+
+/* R1: copy the used slots (and wall slots) to the *_old buffers */
+__global__ void k_copy_old(const int* __restrict__ nebor, const int* __restrict__ num_nebor,
+                           const int* __restrict__ nidx, const int* __restrict__ plevel,
+                           const int* __restrict__ npars, const int* __restrict__ nneb,
+                           const ContactRec* __restrict__ rec, const unsigned char* __restrict__ brg,
+                           const int* __restrict__ wlist, const int* __restrict__ nwall,
+                           const ContactRec* __restrict__ wrec, int* __restrict__ nebor_old,
+                           int* __restrict__ num_nebor_old, int* __restrict__ nidx_old,
+                           ContactRec* __restrict__ rec_old, unsigned char* __restrict__ brg_old,
+                           int* __restrict__ wlist_old, int* __restrict__ nwall_old,
+                           ContactRec* __restrict__ wrec_old, int n, unsigned long long* counters) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p == 0 && counters) counters[4] += 1; /* rebuilds */
+  if (p >= n) return;
+  const int L = plevel[p];
+  const long long stride = npars[L];
+  const long long base = slot_base(L, npars, nneb) + nidx[p];
+  const int nn = num_nebor[p];
+  for (int a = 0; a < nn; a++) {
+    const long long s = base + a * stride;
+    nebor_old[s] = nebor[s];
+    rec_old[s] = rec[s];
+    brg_old[s] = brg[s];
+  }
+  num_nebor_old[p] = nn;
+  nidx_old[p] = nidx[p];
+  const int nw = nwall[p];
+  nwall_old[p] = nw;
+  for (int a = 0; a < nw; a++) {
+    wlist_old[3 * p + a] = wlist[3 * p + a];
+    wrec_old[(long long)a * n + p] = wrec[(long long)a * n + p];
+  }
+}
+
+/* R3: gather the particle state into sorted order */
+__global__ void k_permute(const int* __restrict__ src, int n, const double3* __restrict__ pos,
+                          const double3* __restrict__ vel, const double3* __restrict__ angv,
+                          const double* __restrict__ rad, const int* __restrict__ lqd, const int* __restrict__ id,
+                          const int* __restrict__ plevel, double3* __restrict__ tpos, double3* __restrict__ tvel,
+                          double3* __restrict__ tangv, double* __restrict__ trad, int* __restrict__ tlqd,
+                          int* __restrict__ tid, int* __restrict__ tplevel, int* __restrict__ old_to_new) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int p = src[q];
+  tpos[q] = pos[p];
+  tvel[q] = vel[p];
+  tangv[q] = angv[p];
+  trad[q] = rad[p];
+  tlqd[q] = lqd[p];
+  tid[q] = id[p];
+  tplevel[q] = plevel[p];
+  old_to_new[p] = q;
+}
+
+struct LevelStart {
+  int v[DEM_MAX_LEVELS];   /* first sorted position of each level */
+  int cnt[DEM_MAX_LEVELS]; /* particles per level */
+};
+
+/* R3b: copy back, recompute the level rank (sorted order is level-major), clear the path length */
+__global__ void k_copy_back(int n, const double3* __restrict__ tpos, const double3* __restrict__ tvel,
+                            const double3* __restrict__ tangv, const double* __restrict__ trad,
+                            const int* __restrict__ tlqd, const int* __restrict__ tid,
+                            const int* __restrict__ tplevel, double3* __restrict__ pos, double3* __restrict__ vel,
+                            double3* __restrict__ angv, double* __restrict__ rad, int* __restrict__ lqd,
+                            int* __restrict__ id, int* __restrict__ plevel, int* __restrict__ nidx,
+                            double* __restrict__ pmove, LevelStart ls, int* __restrict__ err) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  pos[q] = tpos[q];
+  vel[q] = tvel[q];
+  angv[q] = tangv[q];
+  rad[q] = trad[q];
+  lqd[q] = tlqd[q];
+  id[q] = tid[q];
+  const int L = tplevel[q];
+  plevel[q] = L;
+  int r = q - ls.v[L];
+  /* a particle hashed into another level's cell range (only possible on the
+   * far face of the grid) would break level-major order */
+  if (r < 0 || r >= ls.cnt[L]) {
+    atomicOr(err, 4);
+    r = 0;
+  }
+  nidx[q] = r;
+  pmove[q] = 0.0;
+}
+
+/* R6: carry-over into the new lists: matched slot -> copy, else zero */
+__global__ void k_carry(const int* __restrict__ nebor, const int* __restrict__ num_nebor, const int* __restrict__ nidx,
+                        const int* __restrict__ plevel, const int* __restrict__ npars, const int* __restrict__ nneb,
+                        const int* __restrict__ nebor_old, const int* __restrict__ num_nebor_old,
+                        const int* __restrict__ nidx_old, const ContactRec* __restrict__ rec_old,
+                        const unsigned char* __restrict__ brg_old, ContactRec* __restrict__ rec,
+                        unsigned char* __restrict__ brg, const int* __restrict__ wlist, const int* __restrict__ nwall,
+                        const int* __restrict__ wlist_old, const int* __restrict__ nwall_old,
+                        const ContactRec* __restrict__ wrec_old, ContactRec* __restrict__ wrec,
+                        const int* __restrict__ src, const int* __restrict__ old_to_new, int n) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int p = src ? src[q] : q;
+  const int L = plevel[q];
+  const long long stride = npars[L];
+  const long long lb = slot_base(L, npars, nneb);
+  const long long nb = lb + nidx[q], ob = lb + nidx_old[p];
+  const int nn = num_nebor[q], no = num_nebor_old[p];
+  ContactRec zero;
+  zero.dx = zero.dy = zero.dz = zero.nDsp = zero.nDsp_mx = zero.plstRad = zero.plstDfm = 0.0;
+  zero.stage = 0;
+  for (int a = 0; a < nn; a++) {
+    const long long s = nb + a * stride;
+    const int partner = nebor[s];
+    long long hit = -1;
+    for (int b = 0; b < no; b++) {
+      const long long t = ob + b * stride;
+      int j = nebor_old[t];
+      if (old_to_new) j = old_to_new[j];
+      if (j == partner) hit = t; /* the reference lets the last match win */
+    }
+    if (hit >= 0) {
+      rec[s] = rec_old[hit];
+      brg[s] = brg_old[hit];
+    } else {
+      rec[s] = zero;
+      brg[s] = 0;
+    }
+  }
+  const int nw = nwall[q], nwo = nwall_old[p];
+  for (int a = 0; a < nw; a++) {
+    const int w = wlist[3 * q + a];
+    long long hit = -1;
+    for (int b = 0; b < nwo; b++)
+      if (wlist_old[3 * p + b] == w) hit = (long long)b * n + p;
+    wrec[(long long)a * n + q] = hit >= 0 ? wrec_old[hit] : zero;
+  }
+}
+
+/* device-side rebuild decision: the IF node runs the rebuild when the last
+ * integration flagged a particle or the host asked for one; the flag is then
+ * cleared for this step's integrator to set again */
+__global__ void k_decide(cudaGraphConditionalHandle h, int* flag, int* need) {
+  const unsigned v = (*flag > 0 || *need != 0) ? 1u : 0u;
+  *flag = 0;
+  *need = 0;
+  cudaGraphSetConditional(h, v);
+}
+
+__global__ void k_import(int n, const int* __restrict__ id, const double3* __restrict__ hp,
+                         const double3* __restrict__ hv, const double3* __restrict__ hw, double3* __restrict__ pos,
+                         double3* __restrict__ vel, double3* __restrict__ angv, int has_v, int has_w) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = id[q];
+  pos[q] = hp[i];
+  vel[q] = has_v ? hv[i] : make_double3(0.0, 0.0, 0.0);
+  angv[q] = has_w ? hw[i] : make_double3(0.0, 0.0, 0.0);
+}
+
+__global__ void k_export(int n, const int* __restrict__ id, const double3* __restrict__ src, double3* __restrict__ dst) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  dst[id[q]] = src[q];
+}
+
+__global__ void k_check_finite(int n, const double3* __restrict__ pos, const double3* __restrict__ vel,
+                               int* __restrict__ err) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double3 p = pos[q], v = vel[q];
+  if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z)))
+    atomicOr(err, 2);
+}
+
+/* ------------------------------------------------------------------ */
+
+HistAoS hist_pp(dem_ctx* c) { return HistAoS{c->b.rec, c->b.brg}; }
+HistAoS hist_pw(dem_ctx* c) { return HistAoS{c->b.wrec, nullptr}; }
+
+/* The whole rebuild, enqueued on s (graph-capturable: fixed pointers, no host sync). */
+dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
+  EngineBufs& b = c->b;
+  const int n = c->n;
+  const bool reorder = c->opt.reorder != 0;
+  dem_status st;
+  if (c->opt.precision == DEM_PREC_MIXED) {
+    st = mixed_pre_rebuild(c, parity, s);
+    if (st != DEM_OK) return st;
+  }
+  k_copy_old<<<grid_for(n, 128), 128, 0, s>>>(b.nebor, b.num_nebor, b.nidx, b.plevel, b.npars, b.nneb, b.rec, b.brg,
+                                               b.wlist, b.nwall, b.wrec, b.nebor_old, b.num_nebor_old, b.nidx_old,
+                                               b.rec_old, b.brg_old, b.wlist_old, b.nwall_old, b.wrec_old, n,
+                                               b.counters);
+  st = cell_sort(b.pos, b.plevel, reorder ? b.id : nullptr, n, c->lv, c->k, c->s.sys_ncells, b.sorted_hash,
+                 b.sorted_src, b.cell_start, b.cell_end, b.scratch, b.err, s);
+  if (st != DEM_OK) return st;
+  if (reorder) {
+    k_permute<<<grid_for(n, 256), 256, 0, s>>>(b.sorted_src, n, b.pos, b.vel, b.angv, b.rad, b.lqd, b.id, b.plevel,
+                                                b.tmp_pos, b.tmp_vel, b.tmp_angv, b.tmp_rad, b.tmp_lqd, b.tmp_id,
+                                                b.tmp_plevel, b.old_to_new);
+    LevelStart ls;
+    for (int l = 0; l < DEM_MAX_LEVELS; l++) {
+      ls.v[l] = l < c->s.n_levels ? c->lstart[l] : 0;
+      ls.cnt[l] = l < c->s.n_levels ? c->s.level_npars[l] : 0;
+    }
+    k_copy_back<<<grid_for(n, 256), 256, 0, s>>>(n, b.tmp_pos, b.tmp_vel, b.tmp_angv, b.tmp_rad, b.tmp_lqd, b.tmp_id,
+                                                  b.tmp_plevel, b.pos, b.vel, b.angv, b.rad, b.lqd, b.id, b.plevel,
+                                                  b.nidx, b.pmove, ls, b.err);
+  } else {
+    cudaError_t e = cudaMemsetAsync(b.pmove, 0, sizeof(double) * (size_t)n, s);
+    if (e != cudaSuccess) return cuda_check(e, "pmove reset");
+  }
+  st = neighbor_find(b.pos, b.rad, reorder ? nullptr : b.sorted_src, b.cell_start, b.cell_end, b.plevel, b.nidx,
+                     c->lv, c->k, b.nebor, b.num_nebor, n, b.err, s);
+  if (st != DEM_OK) return st;
+  st = wall_list(b.pos, b.rad, b.cyl, b.wlist, 3 * sizeof(int), b.nwall, n, c->k, s);
+  if (st != DEM_OK) return st;
+  k_carry<<<grid_for(n, 128), 128, 0, s>>>(b.nebor, b.num_nebor, b.nidx, b.plevel, b.npars, b.nneb, b.nebor_old,
+                                           b.num_nebor_old, b.nidx_old, b.rec_old, b.brg_old, b.rec, b.brg, b.wlist,
+                                           b.nwall, b.wlist_old, b.nwall_old, b.wrec_old, b.wrec,
+                                           reorder ? b.sorted_src : nullptr, reorder ? b.old_to_new : nullptr, n);
+  st = cuda_check(cudaGetLastError(), "rebuild launch");
+  if (st != DEM_OK) return st;
+  if (c->opt.precision == DEM_PREC_MIXED) return mixed_shadows(c, parity, s);
+  return DEM_OK;
+}
+
+/* One step's force + integration kernels (graph-capturable). */
+dem_status enqueue_step(dem_ctx* c, cudaStream_t s, int parity) {
+  EngineBufs& b = c->b;
+  const int n = c->n;
+  if (c->opt.precision == DEM_PREC_MIXED) return mixed_step(c, parity, s);
+  dem_status st = var_init(b.force, b.mom, b.rmom, b.lqd, b.lqd_old, n, s);
+  if (st != DEM_OK) return st;
+  st = pp_force64<HistAoS>(b.pos, b.vel, b.angv, b.rad, b.nebor, b.plevel, b.npars, b.nneb, b.nidx, hist_pp(c),
+                           b.num_nebor, b.lqd, b.lqd_old, b.force, b.mom, b.rmom, n, c->s.force_cap,
+                           c->s.load_stage, c->k, b.counters, s);
+  if (st != DEM_OK) return st;
+  st = wall_force64<HistAoS>(b.pos, b.vel, b.angv, b.force, b.mom, b.rmom, b.rad, b.cyl, hist_pw(c), b.nwall,
+                             b.wlist, 3 * sizeof(int), n, n, c->s.load_stage, c->k, b.counters,
+                             c->s.cyl.topv != 0.0, s);
+  if (st != DEM_OK) return st;
+  return update64(b.rad, b.pos, b.vel, b.angv, b.force, b.mom, b.rmom, b.flag, b.pmove, n, c->k, s);
+}
+
+void destroy_graph(dem_ctx* c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  c->graph_exec = nullptr;
+  c->graph_steps = 0;
+}
+
+/* G steps: [decide -> IF(rebuild) -> step] x G, parity alternating from 0 */
+dem_status build_graph(dem_ctx* c, int G) {
+  destroy_graph(c);
+  cudaStream_t cs;
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_check(e, "capture stream");
+  cudaGraph_t g = nullptr;
+  dem_status st = DEM_OK;
+  auto ck = [&](cudaError_t err, const char* what) {
+    if (st == DEM_OK && err != cudaSuccess) st = cuda_check(err, what);
+    return st == DEM_OK;
+  };
+  if (!ck(cudaGraphCreate(&g, 0), "cudaGraphCreate")) {
+    cudaStreamDestroy(cs);
+    return st;
+  }
+  cudaGraphNode_t prev = nullptr;
+  for (int step = 0; step < G && st == DEM_OK; step++) {
+    const int parity = (c->opt.precision == DEM_PREC_MIXED) ? (step & 1) : 0;
+    cudaGraphConditionalHandle h;
+    if (!ck(cudaGraphConditionalHandleCreate(&h, g, 0, 0), "conditional handle")) break;
+    cudaGraphNode_t nd;
+    cudaKernelNodeParams kp;
+    std::memset(&kp, 0, sizeof(kp));
+    void* args[3] = {&h, &c->b.flag, &c->b.need};
+    kp.func = (void*)k_decide;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.kernelParams = args;
+    if (!ck(cudaGraphAddKernelNode(&nd, g, prev ? &prev : nullptr, prev ? 1 : 0, &kp), "decide node")) break;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t nc;
+    if (!ck(cudaGraphAddNode(&nc, g, &nd, nullptr, 1, &cp), "conditional node")) break;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if (!ck(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+            "capture rebuild"))
+      break;
+    dem_status rs = enqueue_rebuild(c, cs, parity);
+    cudaGraph_t body_out = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(cs, &body_out);
+    if (rs != DEM_OK) {
+      st = rs;
+      break;
+    }
+    if (!ck(ee, "end capture rebuild")) break;
+    cudaGraph_t sg = nullptr;
+    if (!ck(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "capture step")) break;
+    dem_status ss = enqueue_step(c, cs, parity);
+    ee = cudaStreamEndCapture(cs, &sg);
+    if (ss != DEM_OK) {
+      st = ss;
+      if (sg) cudaGraphDestroy(sg);
+      break;
+    }
+    if (!ck(ee, "end capture step")) break;
+    cudaGraphNode_t ns;
+    ck(cudaGraphAddChildGraphNode(&ns, g, &nc, 1, sg), "step node");
+    cudaGraphDestroy(sg);
+    prev = ns;
+  }
+  if (st == DEM_OK) {
+    cudaGraphExec_t ex = nullptr;
+    if (ck(cudaGraphInstantiate(&ex, g, 0), "cudaGraphInstantiate")) {
+      c->graph_exec = ex;
+      c->graph_steps = G;
+    }
+  }
+  cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
+  return st;
+}
+
+/* one host-driven step: read the flag, rebuild if needed, step */
+dem_status host_step(dem_ctx* c) {
+  int hv[2] = {0, 0};
+  cudaError_t e = cudaMemcpyAsync(&hv[0], c->b.flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hv[1], c->b.need, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_check(e, "flag read");
+  e = cudaMemsetAsync(c->b.flag, 0, sizeof(int), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->b.need, 0, sizeof(int), c->stream);
+  if (e != cudaSuccess) return cuda_check(e, "flag reset");
+  dem_status st;
+  if (hv[0] > 0 || hv[1] != 0) {
+    st = enqueue_rebuild(c, c->stream, c->parity);
+    if (st != DEM_OK) return st;
+  }
+  st = enqueue_step(c, c->stream, c->parity);
+  if (st != DEM_OK) return st;
+  if (c->opt.precision == DEM_PREC_MIXED) c->parity ^= 1;
+  c->iter++;
+  c->ctime += c->s.sim.dt;
+  return DEM_OK;
+}
+
+constexpr int kGraphSteps = 16;
+
+}  // namespace
+}  // namespace dem
+
+using namespace dem;
+
+extern "C" void dem_default_options(dem_options* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->precision = DEM_PREC_MIXED;
+  o->capillary = DEM_CAP_FORMULA;
+  o->block_size = 0;
+  o->reorder = 1;
+  o->use_graph = 1;
+}
+
+extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const int* plevel, const int* nebor_idx,
+                                 const dem_options* opt, dem_ctx** out) {
+  if (!s || !rad || !plevel || !nebor_idx || !out) return fail(DEM_ERR_ARG, "dem_create: null argument");
+  *out = nullptr;
+  if (s->np <= 0 || s->n_levels < 1 || s->n_levels > DEM_MAX_LEVELS || s->sys_ncells <= 0 || s->n_pp_slots <= 0)
+    return fail(DEM_ERR_ARG, "dem_create: set-up sizes out of range");
+  dem_ctx* c = new dem_ctx();
+  c->s = *s;
+  if (opt) c->opt = *opt;
+  else dem_default_options(&c->opt);
+  if (c->opt.precision == DEM_PREC_MIXED && !c->opt.reorder) {
+    delete c;
+    return fail(DEM_ERR_ARG, "dem_create: the mixed-precision path needs reorder = 1");
+  }
+  c->n = s->np;
+  c->slots = s->n_pp_slots;
+  c->mx = nullptr;
+  c->graph_exec = nullptr;
+  c->graph_steps = 0;
+  c->parity = 0;
+  c->iter = 0;
+  c->ctime = 0.0;
+  std::memcpy(c->k.mat, s->mat, sizeof(c->k.mat));
+  c->k.lqd = s->lqd;
+  c->k.prm = s->prm;
+  c->k.cal = s->cal;
+  std::memcpy(&c->k.pwcal, &s->pwcal, sizeof(calParaPP));
+  int acc = 0;
+  for (int l = 0; l < DEM_MAX_LEVELS; l++) {
+    c->lstart[l] = acc;
+    if (l < s->n_levels) acc += s->level_npars[l];
+  }
+  if (acc != s->np) {
+    delete c;
+    return fail(DEM_ERR_ARG, "dem_create: level particle counts do not add up to np");
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_check(e, "cudaStreamCreate");
+  }
+  EngineBufs& b = c->b;
+  std::memset(&b, 0, sizeof(b));
+  const size_t N = (size_t)c->n, S = (size_t)c->slots, C = (size_t)s->sys_ncells, L = (size_t)s->n_levels;
+  dem_status st = DEM_OK;
+#define A(ptr, count) \
+  if (st == DEM_OK) st = dalloc(c, &(ptr), (count))
+  A(b.pos, N); A(b.vel, N); A(b.angv, N); A(b.rad, N); A(b.pmove, N); A(b.lqd, N); A(b.lqd_old, N);
+  A(b.id, N); A(b.plevel, N); A(b.nidx, N);
+  A(b.tmp_pos, N); A(b.tmp_vel, N); A(b.tmp_angv, N); A(b.tmp_rad, N); A(b.tmp_lqd, N); A(b.tmp_id, N);
+  A(b.tmp_plevel, N);
+  A(b.force, N); A(b.mom, N); A(b.rmom, N);
+  A(b.nebor, S); A(b.num_nebor, N); A(b.wlist, 3 * N); A(b.nwall, N);
+  A(b.nebor_old, S); A(b.num_nebor_old, N); A(b.wlist_old, 3 * N); A(b.nwall_old, N); A(b.nidx_old, N);
+  A(b.rec, S); A(b.rec_old, S); A(b.brg, S); A(b.brg_old, S); A(b.wrec, 3 * N); A(b.wrec_old, 3 * N);
+  A(b.sorted_hash, N); A(b.sorted_src, N); A(b.old_to_new, N); A(b.cell_start, C); A(b.cell_end, C);
+  A(b.cell_size, L); A(b.grid_size, L); A(b.ncell_idx, L); A(b.npars, L); A(b.nneb, L); A(b.level_size, L);
+  A(b.cyl, 1); A(b.flag, 1); A(b.need, 1); A(b.err, 1); A(b.counters, 8);
+#undef A
+  if (st == DEM_OK) {
+    void* sc = nullptr;
+    st = cuda_alloc(&sc, sort_scratch_bytes(c->n, s->sys_ncells));
+    if (st == DEM_OK) {
+      c->allocs.push_back(sc);
+      b.scratch = sc;
+    }
+  }
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (st != DEM_OK) return;
+    cudaError_t ee = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    if (ee != cudaSuccess) st = cuda_check(ee, "upload");
+  };
+  up(b.cell_size, s->cell_size, sizeof(double) * L);
+  up(b.grid_size, s->grid_size, sizeof(int3) * L);
+  up(b.ncell_idx, s->ncell_idx, sizeof(int) * L);
+  up(b.npars, s->level_npars, sizeof(int) * L);
+  up(b.nneb, s->level_nnebors, sizeof(int) * L);
+  up(b.level_size, s->level_size, sizeof(double) * L);
+  up(b.cyl, &s->cyl, sizeof(CylinderBC));
+  up(b.rad, rad, sizeof(double) * N);
+  up(b.plevel, plevel, sizeof(int) * N);
+  if (st == DEM_OK) {
+    std::vector<int> ids(N);
+    for (size_t i = 0; i < N; i++) ids[i] = (int)i;
+    up(b.id, ids.data(), sizeof(int) * N);
+  }
+  up(b.nidx, nebor_idx, sizeof(int) * N);
+  const int one = 1;
+  up(b.need, &one, sizeof(int));
+  c->lv.cell_size = b.cell_size;
+  c->lv.grid_size = b.grid_size;
+  c->lv.ncell_idx = b.ncell_idx;
+  c->lv.level_size = b.level_size;
+  c->lv.level_npars = b.npars;
+  c->lv.level_nnebors = b.nneb;
+  c->lv.n_levels = s->n_levels;
+  if (st == DEM_OK && c->opt.precision == DEM_PREC_MIXED) st = mixed_create(c);
+  if (st != DEM_OK) {
+    dem_destroy(c);
+    return st;
+  }
+  *out = c;
+  return DEM_OK;
+}
+
+extern "C" dem_status dem_destroy(dem_ctx* c) {
+  if (!c) return DEM_OK;
+  cudaStreamSynchronize(c->stream);
+  destroy_graph(c);
+  if (c->mx) mixed_destroy(c);
+  for (void* p : c->allocs) cudaFree(p);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return DEM_OK;
+}
+
+extern "C" void* dem_stream(dem_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel) {
+  if (!c || !pos) return fail(DEM_ERR_ARG, "dem_set_state: null argument");
+  const size_t N = (size_t)c->n;
+  EngineBufs& b = c->b;
+  /* host arrays (caller order) go to the tmp buffers, then a gather by id */
+  cudaError_t e = cudaMemcpyAsync(b.tmp_pos, pos, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess && vel) e = cudaMemcpyAsync(b.tmp_vel, vel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess && angvel)
+    e = cudaMemcpyAsync(b.tmp_angv, angvel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_check(e, "dem_set_state upload");
+  k_import<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_pos, b.tmp_vel, b.tmp_angv, b.pos, b.vel,
+                                                         b.angv, vel != nullptr, angvel != nullptr);
+  const int one = 1;
+  e = cudaMemcpyAsync(b.need, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return cuda_check(e, "dem_set_state");
+}
+
+extern "C" dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,
+                                    double3* mom) {
+  if (!c) return fail(DEM_ERR_ARG, "dem_get_state: null context");
+  EngineBufs& b = c->b;
+  const size_t N = (size_t)c->n;
+  if (c->opt.precision == DEM_PREC_MIXED && (force || mom)) {
+    dem_status st = mixed_force_to_master(c, c->stream);
+    if (st != DEM_OK) return st;
+  }
+  struct Item {
+    double3* host;
+    const double3* dev;
+  } items[5] = {{pos, b.pos}, {vel, b.vel}, {angvel, b.angv}, {force, b.force}, {mom, b.mom}};
+  for (auto& it : items) {
+    if (!it.host) continue;
+    k_export<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, it.dev, b.tmp_pos);
+    cudaError_t e = cudaMemcpyAsync(it.host, b.tmp_pos, sizeof(double3) * N, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_check(e, "dem_get_state");
+  }
+  return DEM_OK;
+}
+
+extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
+  if (!c || nsteps < 0) return fail(DEM_ERR_ARG, "dem_step: bad argument");
+  dem_status st = DEM_OK;
+  int left = nsteps;
+  if (c->opt.use_graph) {
+    /* graph replays start at shadow parity 0 */
+    if (c->parity != 0 && left > 0) {
+      st = host_step(c);
+      if (st != DEM_OK) return st;
+      left--;
+    }
+    if (left >= kGraphSteps) {
+      if (!c->graph_exec) {
+        st = build_graph(c, kGraphSteps);
+        if (st != DEM_OK) return st;
+      }
+      while (left >= kGraphSteps) {
+        cudaError_t e = cudaGraphLaunch(c->graph_exec, c->stream);
+        if (e != cudaSuccess) return cuda_check(e, "cudaGraphLaunch");
+        left -= kGraphSteps;
+        c->iter += kGraphSteps;
+        c->ctime += kGraphSteps * c->s.sim.dt;
+      }
+    }
+  }
+  while (left > 0) {
+    st = host_step(c);
+    if (st != DEM_OK) return st;
+    left--;
+  }
+  return DEM_OK;
+}
+
+extern "C" dem_status dem_sync(dem_ctx* c) {
+  if (!c) return fail(DEM_ERR_ARG, "dem_sync: null context");
+  k_check_finite<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->b.pos, c->b.vel, c->b.err);
+  int err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, c->b.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_check(e, "dem_sync");
+  if (err & 1) return fail(DEM_ERR_OVERFLOW, "a neighbour list ran past its level's slot capacity");
+  if (err & 2) return fail(DEM_ERR_NONFINITE, "non-finite particle state");
+  if (err & 4) return fail(DEM_ERR_CELL, "a particle left the cell grid");
+  return DEM_OK;
+}
+
+extern "C" dem_status dem_get_stats(dem_ctx* c, dem_stats* st) {
+  if (!c || !st) return fail(DEM_ERR_ARG, "dem_get_stats: null argument");
+  unsigned long long ctr[8];
+  int err = 0;
+  cudaError_t e = cudaMemcpyAsync(ctr, c->b.counters, sizeof(ctr), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err, c->b.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_check(e, "dem_get_stats");
+  std::memset(st, 0, sizeof(*st));
+  st->iter = c->iter;
+  st->rebuilds = (long long)ctr[4];
+  st->nb_entries = (long long)ctr[0];
+  st->contacts = (long long)ctr[1];
+  st->bridges = (long long)ctr[2];
+  st->wall_contacts = (long long)ctr[3];
+  st->error_bits = err;
+  st->ctime = c->ctime;
+  return DEM_OK;
+}
+
+extern "C" dem_status dem_get_neighbors(dem_ctx* c, int* counts, int* partners, int max_per) {
+  if (!c || !counts || !partners || max_per <= 0) return fail(DEM_ERR_ARG, "dem_get_neighbors: bad argument");
+  const size_t N = (size_t)c->n, S = (size_t)c->slots;
+  std::vector<int> nebor(S), num(N), nidx(N), plevel(N), id(N);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(nebor.data(), c->b.nebor, sizeof(int) * S, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(num.data(), c->b.num_nebor, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(nidx.data(), c->b.nidx, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(plevel.data(), c->b.plevel, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(id.data(), c->b.id, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_check(e, "dem_get_neighbors");
+  long long base[DEM_MAX_LEVELS];
+  long long acc = 0;
+  for (int l = 0; l < c->s.n_levels; l++) {
+    base[l] = acc;
+    acc += (long long)c->s.level_nnebors[l] * c->s.level_npars[l];
+  }
+  for (size_t q = 0; q < N; q++) {
+    const int i = id[q], L = plevel[q];
+    if (num[q] > max_per) return fail(DEM_ERR_ARG, "dem_get_neighbors: max_per too small");
+    counts[i] = num[q];
+    for (int a = 0; a < num[q]; a++) {
+      const long long sl = base[L] + (long long)a * c->s.level_npars[L] + nidx[q];
+      partners[(size_t)i * max_per + a] = id[nebor[sl]];
+    }
+  }
+  return DEM_OK;
+}
+
+extern "C" dem_status dem_get_history(dem_ctx* c, double* rec, int* brg, int max_per) {
+  if (!c || !rec || max_per <= 0) return fail(DEM_ERR_ARG, "dem_get_history: bad argument");
+  const size_t N = (size_t)c->n, S = (size_t)c->slots;
+  std::vector<ContactRec> r(S);
+  std::vector<unsigned char> bf(S);
+  std::vector<int> num(N), nidx(N), plevel(N), id(N);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(r.data(), c->b.rec, sizeof(ContactRec) * S, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(bf.data(), c->b.brg, S, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(num.data(), c->b.num_nebor, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(nidx.data(), c->b.nidx, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(plevel.data(), c->b.plevel, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(id.data(), c->b.id, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_check(e, "dem_get_history");
+  long long base[DEM_MAX_LEVELS];
+  long long acc = 0;
+  for (int l = 0; l < c->s.n_levels; l++) {
+    base[l] = acc;
+    acc += (long long)c->s.level_nnebors[l] * c->s.level_npars[l];
+  }
+  for (size_t q = 0; q < N; q++) {
+    const int i = id[q], L = plevel[q];
+    if (num[q] > max_per) return fail(DEM_ERR_ARG, "dem_get_history: max_per too small");
+    for (int a = 0; a < num[q]; a++) {
+      const long long sl = base[L] + (long long)a * c->s.level_npars[L] + nidx[q];
+      double* o = rec + ((size_t)i * max_per + a) * 8;
+      const ContactRec& x = r[(size_t)sl];
+      o[0] = x.dx; o[1] = x.dy; o[2] = x.dz; o[3] = x.nDsp; o[4] = x.nDsp_mx; o[5] = x.plstRad;
+      o[6] = x.plstDfm; o[7] = (double)(int)(x.stage & 0xffffffff);
+      if (brg) brg[(size_t)i * max_per + a] = bf[(size_t)sl];
+    }
+  }
+  return DEM_OK;
+}
+
+/* ---------------- checkpoint ---------------- */
+namespace {
+struct Blob {
+  void* dev;
+  size_t bytes;
+};
+std::vector<Blob> checkpoint_blobs(dem_ctx* c) {
+  EngineBufs& b = c->b;
+  const size_t N = (size_t)c->n, S = (size_t)c->slots;
+  return {{b.pos, sizeof(double3) * N}, {b.vel, sizeof(double3) * N}, {b.angv, sizeof(double3) * N},
+          {b.rad, sizeof(double) * N},  {b.pmove, sizeof(double) * N}, {b.lqd, sizeof(int) * N},
+          {b.id, sizeof(int) * N},      {b.plevel, sizeof(int) * N},   {b.nidx, sizeof(int) * N},
+          {b.nebor, sizeof(int) * S},   {b.num_nebor, sizeof(int) * N}, {b.wlist, sizeof(int) * 3 * N},
+          {b.nwall, sizeof(int) * N},   {b.rec, sizeof(ContactRec) * S}, {b.brg, S},
+          {b.wrec, sizeof(ContactRec) * 3 * N}, {b.flag, sizeof(int)}, {b.need, sizeof(int)},
+          {b.cyl, sizeof(CylinderBC)}, {b.counters, sizeof(unsigned long long) * 8}};
+}
+const char kMagic[8] = {'D', 'E', 'M', 'G', 'B', '3', '0', '1'};
+}  // namespace
+
+extern "C" dem_status dem_save(dem_ctx* c, const char* path, int nBatch) {
+  if (!c || !path) return fail(DEM_ERR_ARG, "dem_save: null argument");
+  dem_status st = DEM_OK;
+  if (c->opt.precision == DEM_PREC_MIXED && c->parity != 0)
+    return fail(DEM_ERR_STATE, "dem_save: call after an even number of steps");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_check(e, "dem_save");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(DEM_ERR_IO, std::string("cannot write ") + path);
+  /* the text header LoadPara reads (DumpLoad.cpp:14-17) */
+  std::fprintf(f, "SYSTEM Info\n%d %d %d\n", c->n, nBatch, c->n);
+  std::fwrite(kMagic, 1, 8, f);
+  long long hdr[4] = {c->iter, (long long)c->n, c->slots, (long long)c->opt.precision};
+  std::fwrite(hdr, sizeof(hdr), 1, f);
+  std::fwrite(&c->ctime, sizeof(double), 1, f);
+  for (const Blob& bl : checkpoint_blobs(c)) {
+    std::vector<char> h(bl.bytes);
+    e = cudaMemcpy(h.data(), bl.dev, bl.bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      st = cuda_check(e, "dem_save copy");
+      break;
+    }
+    if (std::fwrite(h.data(), 1, bl.bytes, f) != bl.bytes) {
+      st = fail(DEM_ERR_IO, "dem_save: short write");
+      break;
+    }
+  }
+  std::fclose(f);
+  return st;
+}
+
+extern "C" dem_status dem_load(dem_ctx* c, const char* path) {
+  if (!c || !path) return fail(DEM_ERR_ARG, "dem_load: null argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(DEM_ERR_IO, std::string("cannot read ") + path);
+  int np = 0, nb = 0, tp = 0;
+  char line[64];
+  if (!std::fgets(line, sizeof(line), f) || std::strncmp(line, "SYSTEM Info", 11) != 0 ||
+      std::fscanf(f, "%d %d %d", &np, &nb, &tp) != 3 || std::fgetc(f) != '\n') {
+    std::fclose(f);
+    return fail(DEM_ERR_IO, "dem_load: bad header");
+  }
+  char magic[8];
+  long long hdr[4];
+  double ct = 0.0;
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kMagic, 8) != 0 || std::fread(hdr, sizeof(hdr), 1, f) != 1 ||
+      std::fread(&ct, sizeof(double), 1, f) != 1) {
+    std::fclose(f);
+    return fail(DEM_ERR_IO, "dem_load: bad binary header");
+  }
+  if (hdr[1] != c->n || hdr[2] != c->slots || hdr[3] != c->opt.precision) {
+    std::fclose(f);
+    return fail(DEM_ERR_ARG, "dem_load: checkpoint does not match this context");
+  }
+  dem_status st = DEM_OK;
+  for (const Blob& bl : checkpoint_blobs(c)) {
+    std::vector<char> h(bl.bytes);
+    if (std::fread(h.data(), 1, bl.bytes, f) != bl.bytes) {
+      st = fail(DEM_ERR_IO, "dem_load: truncated checkpoint");
+      break;
+    }
+    cudaError_t e = cudaMemcpy(bl.dev, h.data(), bl.bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      st = cuda_check(e, "dem_load copy");
+      break;
+    }
+  }
+  std::fclose(f);
+  if (st != DEM_OK) return st;
+  c->iter = hdr[0];
+  c->ctime = ct;
+  c->parity = 0;
+  if (c->opt.precision == DEM_PREC_MIXED) st = mixed_shadows(c, 0, c->stream);
+  if (st == DEM_OK) st = cuda_check(cudaStreamSynchronize(c->stream), "dem_load sync");
+  return st;
+}

@@ -1,0 +1,100 @@
+/*
+ * engine.h -- the native engine's context (dem_ctx), shared by engine.cu and mixed.cu.
+ *
+ * Device memory layout (N particles, S neighbour slots, C cells):
+ *  - particle state in cell order (reorder = 1) or caller order: pos, vel,
+ *    angv (FP64 double3), rad, pmove (FP64), lqd (bridge count of the last
+ *    step), id (caller id), plevel, nidx (rank inside the level: the slot
+ *    column), plus tmp_* copies used while permuting;
+ *  - neighbour lists: nebor[S] level/slot-major (slot(q,k) = base[L] +
+ *    k*npars[L] + nidx[q], coalesced across consecutive particles for a fixed
+ *    k), num_nebor[N]; wall lists wlist[N][3], nwall[N];
+ *  - contact history: 64-byte ContactRec per slot (+ one bridge byte), and
+ *    3N wall records (slot (a, q) at a*N + q);
+ *  - *_old copies of the used slots, written at the start of a rebuild and
+ *    read by the carry-over (fixed pointers, so a rebuild can sit inside a
+ *    CUDA-graph conditional node);
+ *  - mixed precision: FP32 shadow state read by neighbours, double-buffered
+ *    per step (see mixed.cu).
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "dem_internal.h"
+
+namespace dem {
+
+struct MixedState; /* mixed.cu */
+
+struct EngineBufs {
+  /* particle state */
+  double3 *pos, *vel, *angv;
+  double *rad, *pmove;
+  int *lqd, *lqd_old, *id, *plevel, *nidx;
+  double3 *tmp_pos, *tmp_vel, *tmp_angv;
+  double* tmp_rad;
+  int *tmp_lqd, *tmp_id, *tmp_plevel;
+  double3 *force, *mom;
+  double* rmom;
+  /* lists */
+  int *nebor, *num_nebor, *wlist, *nwall;
+  int *nebor_old, *num_nebor_old, *wlist_old, *nwall_old, *nidx_old;
+  /* history */
+  ContactRec *rec, *rec_old, *wrec, *wrec_old;
+  unsigned char *brg, *brg_old;
+  /* sort */
+  int *sorted_hash, *sorted_src, *old_to_new, *cell_start, *cell_end;
+  void* scratch;
+  /* level tables */
+  double* cell_size;
+  int3* grid_size;
+  int *ncell_idx, *npars, *nneb;
+  double* level_size;
+  CylinderBC* cyl;
+  /* control words: flag (rebuild count from the integrator), need (host
+   * request), err (error bits), counters (u64[8]) */
+  int *flag, *need, *err;
+  unsigned long long* counters;
+};
+
+}  // namespace dem
+
+struct dem_ctx {
+  dem_setup s;
+  dem_options opt;
+  int n;
+  long long slots;
+  cudaStream_t stream;
+  dem::DevConsts k;
+  dem::LevelView lv;
+  int lstart[DEM_MAX_LEVELS];
+  dem::EngineBufs b;
+  std::vector<void*> allocs;
+  long long iter;
+  long long rebuilds_host;
+  double ctime;
+  dem::MixedState* mx;
+  /* CUDA graphs of a fixed number of steps (even), one per count */
+  cudaGraphExec_t graph_exec;
+  int graph_steps;
+  int parity; /* mixed: which shadow buffer the next step reads */
+};
+
+namespace dem {
+
+/* mixed.cu */
+dem_status mixed_create(dem_ctx* c);
+void mixed_destroy(dem_ctx* c);
+/* regenerate shadow buffer `which` from the FP64 master state */
+dem_status mixed_shadows(dem_ctx* c, int which, cudaStream_t s);
+/* one fused step reading shadows `which`, writing shadows 1 - which */
+dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s);
+/* copy the last step's bridge counts from the shadow `which` to the master */
+dem_status mixed_pre_rebuild(dem_ctx* c, int which, cudaStream_t s);
+/* download the last step's force totals into the FP64 force array */
+dem_status mixed_force_to_master(dem_ctx* c, cudaStream_t s);
+
+}  // namespace dem

@@ -1,0 +1,588 @@
+/*
+ * mixed.cu -- the fused FP32-force / FP64-state step kernel (sm_103a).
+ *
+ * One launch per time step does, for each particle i (cell order, one thread):
+ * gravity, every p-p contact and capillary bridge over i's neighbour slots,
+ * the <= 3 cylinder-wall contacts, and the integrator -- the reference's
+ * VarInit + PPForceCalcG + CirPWInterG + UpdateSystemG (kernel.cu:413-606,
+ * 958-1023) in one pass.
+ *
+ * Why this shape on GB300: FP64 arithmetic runs at ~0.6 T op/s (1/58 of
+ * FP32) and FP64 pow at ~6 G/s, so the reference's all-FP64 pair math is
+ * bound by FP64 issue.  Here:
+ *  - neighbours are read from FP32 "shadow" copies of last step's state
+ *    (double-buffered: step t reads buffer t%2, writes the other), written by
+ *    the integrator, so a neighbour costs one 16-byte gather until it is a
+ *    contact candidate;
+ *  - positions are shadowed as hi + lo float pairs of (x + offset), where the
+ *    offset puts every coordinate in the binade [2^k, 2^(k+1)): hi_i - hi_j
+ *    is then exact (Sterbenz), and the overlap d - (ri + rj) is computed as
+ *    (d^2 - S^2) / (d + S) with d^2 - S^2 accumulated from exact products
+ *    (FMA two-products + two-sums), so the overlap keeps ~1e-7 relative
+ *    accuracy without FP64 operations even though d and S agree to 1e-4;
+ *  - pair forces are FP32, summed per particle with Kahan compensation in
+ *    the reference's neighbour order;
+ *  - FP64 stays for the state (integrator) and for the tangential spring of
+ *    the contact history, which is advanced by FP64 additions of FP32
+ *    increments (projection correction, length-preserving rescale written as
+ *    a small difference, v_t dt) so its accumulation error is relative to
+ *    the increment, not to the spring;
+ *  - contact records are 64 bytes (two DRAM sectors) read and written only for
+ *    contacts; bridge flags are one byte per slot, coalesced across particles.
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "dem_device.cuh"
+#include "engine.h"
+
+namespace dem {
+
+struct MixedState {
+  float4 *phi[2], *plo[2], *vel[2], *angv[2];
+  float4* force;
+  double3 off;
+  float coarse_tol;
+};
+
+namespace {
+
+inline int grid_for(long long n, int block) { return n <= 0 ? 1 : (int)((n + block - 1) / block); }
+
+constexpr float kPiF = 3.1415926f;
+
+/* contact-law constants in FP32 */
+struct Law32 {
+  float emod, pois, sfrc, ydsp, yforce, ystiff;
+  float rot_eps, dsmx_eps;
+  float dmp;     /* sqrt(dmpn product) */
+  int hertz_le;  /* p-p: <=, wall: < */
+  int damp_on;
+};
+
+struct MixArgs {
+  const float4 *phi_in, *plo_in, *v_in, *w_in;
+  float4 *phi_out, *plo_out, *v_out, *w_out;
+  double3 *pos, *vel, *angv;
+  const double* rad;
+  double* pmove;
+  const int *nebor, *num_nebor, *plevel, *nidx, *npars, *nneb;
+  ContactRec* rec;
+  unsigned char* brg;
+  const int *wlist, *nwall;
+  ContactRec* wrec;
+  float4* force_out;
+  int *flag, *err;
+  unsigned long long* counters;
+  const CylinderBC* cyl;
+  int n, force_cap;
+  double3 off;
+  double dt, move_limit; /* 0.3 * SearchGap */
+  float dtf, coarse_tol, rfrc;
+  float lqd_vol, lqd_layer, lqd_gapmn, lqd_st;
+  Law32 pp, pw;
+};
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dotf(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float lenf(float3 a) { return sqrtf(dotf(a, a)); }
+__device__ __forceinline__ float3 crossf(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+/* Kahan-compensated running sum */
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+struct KSum3 {
+  KSum x, y, z;
+  __device__ __forceinline__ void add(float3 v) { x.add(v.x); y.add(v.y); z.add(v.z); }
+};
+
+/* error-free transforms (Knuth two-sum, FMA two-product) */
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+  const float s = a + b;
+  const float bb = s - a;
+  err = (a - (s - bb)) + (b - bb);
+  return s;
+}
+
+/* the elasto-plastic normal law, damping, tangential spring and rolling
+ * resistance of kernel.cu:89-228 / :236-359 in FP32, with the spring held in
+ * FP64 and advanced by FP32 increments */
+__device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, float3 u, float3 cpv, ContactRec& r,
+                                      float iRad, float rfrc, float dt, float3& dF, float3& dM, float& dR) {
+  const float plstDfm0 = (float)r.plstDfm, nDsp0 = (float)r.nDsp, nDspMx0 = (float)r.nDsp_mx;
+  float plstRad = (float)r.plstRad, plstDfm = plstDfm0, nDspMx = nDspMx0;
+  int st;
+  if (nrm < plstDfm0) st = 1;
+  else if (nrm >= plstDfm0 && nrm < nDsp0) st = 3;
+  else if (nrm >= nDsp0 && nrm < nDspMx0) st = 4;
+  else st = 2;
+  float fN = 0.f;
+  const float k43 = 4.0f / 3.0f * c.emod;
+  const float sq = sqrtf(ijRad * nrm);
+  if (st == 2) {
+    const bool elastic = c.hertz_le ? (nrm <= c.ydsp * ijRad) : (nrm < c.ydsp * ijRad);
+    if (elastic) {
+      fN = k43 * sq * nrm;
+      plstRad = ijRad;
+      plstDfm = 0.f;
+    } else {
+      fN = c.yforce * ijRad * ijRad + c.ystiff * ijRad * (nrm - c.ydsp * ijRad);
+      plstRad = ijRad * (k43 * sq * nrm) / fN;
+      const float t = cbrtf(fN / (k43 * sqrtf(ijRad)));
+      plstDfm = nrm - t * t;
+    }
+    nDspMx = nrm;
+  } else if (st != 1) {
+    const float t = nrm - plstDfm0;
+    fN = k43 * sqrtf(plstRad) * (t * sqrtf(t));
+  }
+  const float vn = dotf(cpv, u);
+  const float fD = c.damp_on ? -2.0f * c.dmp * c.emod * sq * vn : 0.f;
+  const float3 vt = cpv - vn * u;
+
+  /* spring: d_new = rescale(project(d)) + v_t dt, as an FP64 update by a
+   * small FP32 increment.  With cq = u.d, the projection is d - u cq and its
+   * length^2 is |d|^2 - cq^2, so the rescale factor minus one is
+   * cq^2 / ((|d| + |p|) |p|). */
+  const double3 d64 = make_double3(r.dx, r.dy, r.dz);
+  const float3 d = f3((float)d64.x, (float)d64.y, (float)d64.z);
+  const float cq = dotf(u, d);
+  const float3 corr = f3(-u.x * cq, -u.y * cq, -u.z * cq);
+  const float ld = lenf(d);
+  const float lp = lenf(d + corr);
+  float3 inc;
+  if (lp > c.rot_eps) {
+    const float sm1 = (cq * cq) / ((ld + lp) * lp);
+    inc = corr * (1.0f + sm1) + d * sm1 + vt * dt;
+  } else {
+    inc = corr + vt * dt;
+  }
+  double3 n64 = make_double3(d64.x + (double)inc.x, d64.y + (double)inc.y, d64.z + (double)inc.z);
+  float3 dn = d + inc;
+  const float dsmx = 3.0f * c.sfrc * fN / (16.0f * (1.0f - c.pois) * c.emod / (4.0f - 2.0f * c.pois) * sq);
+  float ratio = 1.0f;
+  float ldn = lenf(dn);
+  if (ldn < dsmx) {
+    if (dsmx > c.dsmx_eps) {
+      const float t = 1.0f - ldn / dsmx;
+      ratio = 1.0f - t * sqrtf(t);
+    }
+  } else {
+    const float f = (ldn > c.dsmx_eps) ? dsmx / ldn : dsmx;
+    n64.x *= (double)f;
+    n64.y *= (double)f;
+    n64.z *= (double)f;
+    dn = dn * f;
+    ldn = lenf(dn);
+  }
+  r.dx = n64.x;
+  r.dy = n64.y;
+  r.dz = n64.z;
+  float3 fT = f3(0.f, 0.f, 0.f);
+  if (ldn < dsmx) {
+    if (ldn > 1.0e-10f) fT = dn * (-c.sfrc * fN * ratio / ldn);
+  } else {
+    const float lvt = lenf(vt);
+    if (lvt > 1.0e-10f) fT = vt * (-c.sfrc * fN * ratio / lvt);
+  }
+  dF = (fN + fD) * u + fT;
+  const float arm = iRad - nrm * 0.5f;
+  dM = crossf(u * (-arm), fT);
+  dR = 0.5f * (rfrc + rfrc) * fN * iRad;
+  r.nDsp = (double)nrm;
+  r.nDsp_mx = (double)nDspMx;
+  r.plstRad = (double)plstRad;
+  r.plstDfm = (double)plstDfm;
+  r.stage = st;
+}
+
+/* kernel.cu:65-81 in FP32 */
+__device__ __forceinline__ float fcap32(float Splus, float ijVol, float effR, float gapmn, float st) {
+  Splus = fmaxf(gapmn, Splus);
+  Splus = Splus / sqrtf(ijVol);
+  const float L = logf(ijVol), L2 = L * L, L3 = L2 * L;
+  const float f1 = -0.44507f - 0.1119f * L - 0.012101f * L2 - 0.0005f * L3;
+  const float f2 = 1.9222f - 0.0668f * L - 0.0013375f * L2;
+  const float f3 = 1.268f + 0.198f * L + 0.02232f * L2 + 0.0008585f * L3;
+  const float f4 = -0.010703f + 0.03345f * L + 0.0018574f * L2;
+  const float ls = logf(Splus);
+  return 2.0f * kPiF * effR * st * expf(f1 - f2 * expf(f3 * ls + f4 * ls * ls));
+}
+
+__device__ __forceinline__ ContactRec load_rec(const ContactRec* p) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+  const double2 a = q[0], b = q[1], c = q[2], d = q[3];
+  ContactRec r;
+  r.dx = a.x; r.dy = a.y; r.dz = b.x; r.nDsp = b.y; r.nDsp_mx = c.x; r.plstRad = c.y; r.plstDfm = d.x;
+  r.stage = __double_as_longlong(d.y);
+  return r;
+}
+__device__ __forceinline__ void store_rec(ContactRec* p, const ContactRec& r) {
+  double2* q = reinterpret_cast<double2*>(p);
+  q[0] = make_double2(r.dx, r.dy);
+  q[1] = make_double2(r.dz, r.nDsp);
+  q[2] = make_double2(r.nDsp_mx, r.plstRad);
+  q[3] = make_double2(r.plstDfm, __longlong_as_double(r.stage));
+}
+
+__device__ __forceinline__ void warp_add(unsigned long long* ctr, unsigned v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(ctr, (unsigned long long)v);
+}
+
+template <bool WET>
+__global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
+  if (a.n <= 0) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = q < a.n;
+  const int qq = live ? q : a.n - 1;
+
+  const float4 hi = a.phi_in[qq], lo = a.plo_in[qq], vi4 = a.v_in[qq], wi4 = a.w_in[qq];
+  const float ri = hi.w + lo.w;
+  const float3 iv = f3(vi4.x, vi4.y, vi4.z), iw = f3(wi4.x, wi4.y, wi4.z);
+  const float twor = 2.0f * ri;
+  const float mass_f = twor * twor * twor;
+  KSum3 F, M;
+  KSum R;
+  F.z.add(-mass_f); /* gravity, m = (2r)^3 */
+  int wet = 0;
+  float iVol = 0.f;
+  if (WET) {
+    int inl = __float_as_int(vi4.w);
+    if (inl < 12) inl = 12;
+    iVol = a.lqd_vol * mass_f / (float)inl;
+  }
+  const int L = a.plevel[qq];
+  const long long stride = a.npars[L];
+  const long long base = slot_base(L, a.npars, a.nneb) + a.nidx[qq];
+  const int nn = live ? a.num_nebor[qq] : 0;
+  unsigned ncont = 0, nbr = 0;
+  for (int k = 0; k < nn; k++) {
+    const long long s = base + k * stride;
+    const int j = a.nebor[s];
+    const float4 hj = a.phi_in[j];
+    const float ax = hi.x - hj.x, ay = hi.y - hj.y, az = hi.z - hj.z; /* exact */
+    const float shi = hi.w + hj.w;
+    const float coarse = sqrtf(ax * ax + ay * ay + az * az) - shi;
+    float gap = coarse;
+    float3 u = f3(0.f, 0.f, 0.f);
+    float rj = hj.w;
+    const bool cand = WET || coarse < a.coarse_tol;
+    if (cand) {
+      const float4 lj = a.plo_in[j];
+      rj = hj.w + lj.w;
+      const float bx = lo.x - lj.x, by = lo.y - lj.y, bz = lo.z - lj.z;
+      /* d^2 - S^2 from exact pieces */
+      const float px = ax * ax, py = ay * ay, pz = az * az;
+      const float ex = fmaf(ax, ax, -px), ey = fmaf(ay, ay, -py), ez = fmaf(az, az, -pz);
+      float t1, t2, es;
+      const float s1 = two_sum(px, py, t1);
+      const float s2 = two_sum(s1, pz, t2);
+      const float slo = (lo.w + lj.w);
+      const float Sh = two_sum(hi.w, hj.w, es);
+      const float Sl = es + slo;
+      const float qq2 = Sh * Sh, eq = fmaf(Sh, Sh, -qq2);
+      const float s3 = s2 - qq2;
+      const float small = (t1 + t2) + (ex + ey + ez - eq) + 2.0f * (ax * bx + ay * by + az * bz) -
+                          2.0f * Sh * Sl + (bx * bx + by * by + bz * bz) - Sl * Sl;
+      const float D = s3 + small;
+      const float dx = ax + bx, dy = ay + by, dz = az + bz;
+      const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+      gap = D / (dist + (Sh + Sl));
+      const float inv = 1.0f / dist;
+      u = f3(dx * inv, dy * inv, dz * inv);
+      if (gap < 0.f) {
+        const float4 vj4 = a.v_in[j], wj4 = a.w_in[j];
+        const float3 jv = f3(vj4.x, vj4.y, vj4.z), jw = f3(wj4.x, wj4.y, wj4.z);
+        const float3 cpv = (iv - jv) - crossf(iw * ri + jw * rj, u);
+        const float ijRad = ri * rj / (ri + rj);
+        ContactRec rc = load_rec(a.rec + s);
+        float3 dF, dM;
+        float dR;
+        law32(a.pp, ijRad, -gap, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
+        store_rec(a.rec + s, rc);
+        F.add(dF);
+        M.add(dM);
+        R.add(dR);
+        ncont++;
+      }
+    }
+    if (WET) {
+      int jnl = __float_as_int(a.v_in[j].w);
+      if (jnl < 12) jnl = 12;
+      const float tj = 2.0f * rj;
+      const float jVol = a.lqd_vol * (tj * tj * tj) / (float)jnl;
+      float ijVol = iVol + jVol;
+      const float rupture = 0.99f * exp2f(0.33f * log2f(ijVol));
+      int b = a.brg[s];
+      if (gap < 2.0f * a.lqd_layer * (ri + rj)) b = 1;
+      else if (gap > rupture) b = 0;
+      a.brg[s] = (unsigned char)b;
+      if (b) {
+        const float effR = 2.0f * ri * rj / (ri + rj);
+        const float fc = fcap32(gap < 0.f ? 0.f : gap, ijVol * 8.0f, effR, a.lqd_gapmn, a.lqd_st);
+        F.add(u * (-fc));
+        wet++;
+        if (gap >= 0.f) nbr++;
+      }
+    }
+  }
+
+  /* cylinder walls (CirPWInterG), geometry in FP64 */
+  unsigned nwc = 0;
+  double3 p = a.pos[qq];
+  const int nw = live ? a.nwall[qq] : 0;
+  if (nw > 0) {
+    const double rid = a.rad[qq];
+    const CylinderBC cy = *a.cyl;
+    double3 jvel = make_double3(0.0, 0.0, 0.0);
+    for (int w = 0; w < nw; w++) {
+      const int kind = a.wlist[3 * qq + w];
+      double3 jp;
+      if (kind == 0) {
+        jp = make_double3(p.x, p.y, cy.Tw);
+        jvel = make_double3(0.0, 0.0, cy.topv);
+      } else if (kind == 1) {
+        jp = make_double3(p.x, p.y, cy.Bw);
+      } else if (kind == 2) {
+        const double ddx = cy.cir.x - p.x, ddy = cy.cir.y - p.y;
+        const double dist = sqrt(ddx * ddx + ddy * ddy);
+        jp = make_double3(cy.R * ((p.x - cy.cir.x) / dist) + cy.cir.x, cy.R * ((p.y - cy.cir.y) / dist) + cy.cir.y,
+                          p.z);
+      } else {
+        continue;
+      }
+      const double3 d = make_double3(p.x - jp.x, p.y - jp.y, p.z - jp.z);
+      const double len = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+      const float gapw = (float)(len - rid);
+      if (gapw < 0.f) {
+        const float il = (float)(1.0 / len);
+        const float3 u = f3((float)d.x * il, (float)d.y * il, (float)d.z * il);
+        const float3 cpv = (iv - f3((float)jvel.x, (float)jvel.y, (float)jvel.z)) - crossf(iw * ri, u);
+        ContactRec* rp = a.wrec + (long long)w * a.n + qq;
+        ContactRec rc = load_rec(rp);
+        float3 dF, dM;
+        float dR;
+        law32(a.pw, ri, -gapw, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
+        store_rec(rp, rc);
+        F.add(dF);
+        M.add(dM);
+        R.add(dR);
+        nwc++;
+      }
+    }
+  }
+
+  /* integrator (UpdateSystemG) in FP64 with FP32 increments */
+  bool flagged = false;
+  if (live) {
+    const float fx = F.x.s - F.x.c, fy = F.y.s - F.y.c, fz = F.z.s - F.z.c;
+    const float inv_m = a.dtf / mass_f;
+    double3 v = a.vel[q];
+    v.x += (double)(fx * inv_m);
+    v.y += (double)(fy * inv_m);
+    v.z += (double)(fz * inv_m);
+    p.x = fma(v.x, a.dt, p.x);
+    p.y = fma(v.y, a.dt, p.y);
+    p.z = fma(v.z, a.dt, p.z);
+    const float vxf = (float)v.x, vyf = (float)v.y, vzf = (float)v.z;
+    const double pm = a.pmove[q] + (double)(sqrtf(vxf * vxf + vyf * vyf + vzf * vzf) * a.dtf);
+    const float inert = 0.1f * mass_f * twor * twor;
+    const float inv_i = a.dtf / inert;
+    double3 w = a.angv[q];
+    w.x += (double)((M.x.s - M.x.c) * inv_i);
+    w.y += (double)((M.y.s - M.y.c) * inv_i);
+    w.z += (double)((M.z.s - M.z.c) * inv_i);
+    const float rm = (R.s - R.c) * inv_i;
+    const float wxf = (float)w.x, wyf = (float)w.y, wzf = (float)w.z;
+    const float wl = sqrtf(wxf * wxf + wyf * wyf + wzf * wzf);
+    if (wl > 1.0e-7f) {
+      const float f = fminf(1.0f, rm / wl);
+      w.x -= (double)(wxf * f);
+      w.y -= (double)(wyf * f);
+      w.z -= (double)(wzf * f);
+    }
+    a.vel[q] = v;
+    a.pos[q] = p;
+    a.angv[q] = w;
+    a.pmove[q] = pm;
+    flagged = pm > a.move_limit;
+    if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(a.err, 2);
+    /* next step's shadows */
+    const double xo = p.x + a.off.x, yo = p.y + a.off.y, zo = p.z + a.off.z;
+    const float xh = (float)xo, yh = (float)yo, zh = (float)zo;
+    a.phi_out[q] = make_float4(xh, yh, zh, hi.w);
+    a.plo_out[q] = make_float4((float)(xo - (double)xh), (float)(yo - (double)yh), (float)(zo - (double)zh), lo.w);
+    a.v_out[q] = make_float4((float)v.x, (float)v.y, (float)v.z, __int_as_float(wet));
+    a.w_out[q] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
+    a.force_out[q] = make_float4(fx, fy, fz, 0.f);
+  }
+  const unsigned fm = __ballot_sync(0xffffffffu, flagged);
+  if ((threadIdx.x & 31) == 0 && fm) atomicAdd(a.flag, __popc(fm));
+  if (a.counters) {
+    warp_add(&a.counters[0], (unsigned)nn);
+    warp_add(&a.counters[1], ncont);
+    warp_add(&a.counters[2], nbr);
+    warp_add(&a.counters[3], nwc);
+  }
+}
+
+__global__ void k_shadows(int n, const double3* __restrict__ pos, const double3* __restrict__ vel,
+                          const double3* __restrict__ angv, const double* __restrict__ rad, const int* __restrict__ lqd,
+                          double3 off, float4* __restrict__ phi, float4* __restrict__ plo, float4* __restrict__ v4,
+                          float4* __restrict__ w4) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double3 p = pos[q];
+  const double xo = p.x + off.x, yo = p.y + off.y, zo = p.z + off.z;
+  const float xh = (float)xo, yh = (float)yo, zh = (float)zo;
+  const double r = rad[q];
+  const float rh = (float)r;
+  phi[q] = make_float4(xh, yh, zh, rh);
+  plo[q] = make_float4((float)(xo - (double)xh), (float)(yo - (double)yh), (float)(zo - (double)zh),
+                       (float)(r - (double)rh));
+  const double3 v = vel[q], w = angv[q];
+  v4[q] = make_float4((float)v.x, (float)v.y, (float)v.z, __int_as_float(lqd[q]));
+  w4[q] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
+}
+
+__global__ void k_force_out(int n, const float4* __restrict__ f, double3* __restrict__ force, double3* __restrict__ mom) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const float4 v = f[q];
+  force[q] = make_double3(v.x, v.y, v.z);
+  mom[q] = make_double3(0.0, 0.0, 0.0);
+}
+
+__global__ void k_lqd_from_shadow(int n, const float4* __restrict__ v4, int* __restrict__ lqd) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  lqd[q] = __float_as_int(v4[q].w);
+}
+
+Law32 make_law(const calParaPP& c, bool pp, double dmp_sq, int stage) {
+  Law32 l;
+  l.emod = (float)c.emod;
+  l.pois = (float)c.pois;
+  l.sfrc = (float)c.sfrc;
+  l.ydsp = (float)c.ydsp_t;
+  l.yforce = (float)c.yforce_t;
+  l.ystiff = (float)c.ystiff_t;
+  l.rot_eps = pp ? 1.0e-7f : 1.0e-10f;
+  l.dsmx_eps = pp ? 1.0e-7f : 1.0e-10f;
+  l.dmp = (float)std::sqrt(dmp_sq);
+  l.hertz_le = pp ? 1 : 0;
+  l.damp_on = pp ? (stage == 1) : (stage == 1 || stage == 7);
+  return l;
+}
+
+}  // namespace
+
+dem_status mixed_create(dem_ctx* c) {
+  MixedState* m = new MixedState();
+  std::memset(m, 0, sizeof(*m));
+  c->mx = m;
+  const size_t N = (size_t)c->n;
+  float4** bufs[9] = {&m->phi[0], &m->phi[1], &m->plo[0], &m->plo[1], &m->vel[0],
+                      &m->vel[1], &m->angv[0], &m->angv[1], &m->force};
+  for (float4** b : bufs) {
+    void* p = nullptr;
+    dem_status st = cuda_alloc(&p, sizeof(float4) * N);
+    if (st != DEM_OK) return st;
+    cudaMemset(p, 0, sizeof(float4) * N);
+    c->allocs.push_back(p);
+    *b = (float4*)p;
+  }
+  /* offset putting every coordinate of the domain in [2^k, 2^(k+1)) */
+  const PARAMETER& prm = c->s.prm;
+  double ext = std::max(prm.EndPoint.x - prm.Origin.x,
+                        std::max(prm.EndPoint.y - prm.Origin.y, prm.EndPoint.z - prm.Origin.z));
+  int k2 = (int)std::ceil(std::log2(std::max(ext, 1.0) * 1.0001));
+  const double base = std::ldexp(1.0, k2);
+  m->off = make_double3(base - prm.Origin.x, base - prm.Origin.y, base - prm.Origin.z);
+  /* the hi-part-only overlap estimate is off by at most |lo_i - lo_j| per
+   * axis, below two ulps of the binade: four ulps is a safe candidate margin */
+  m->coarse_tol = (float)(4.0 * std::ldexp(1.0, k2 - 23));
+  return DEM_OK;
+}
+
+void mixed_destroy(dem_ctx* c) {
+  delete c->mx;
+  c->mx = nullptr;
+}
+
+dem_status mixed_shadows(dem_ctx* c, int which, cudaStream_t s) {
+  MixedState* m = c->mx;
+  EngineBufs& b = c->b;
+  k_shadows<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, b.pos, b.vel, b.angv, b.rad, b.lqd, m->off, m->phi[which],
+                                                 m->plo[which], m->vel[which], m->angv[which]);
+  return cuda_check(cudaGetLastError(), "mixed_shadows launch");
+}
+
+dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
+  MixedState* m = c->mx;
+  EngineBufs& b = c->b;
+  MixArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.phi_in = m->phi[which]; a.plo_in = m->plo[which]; a.v_in = m->vel[which]; a.w_in = m->angv[which];
+  a.phi_out = m->phi[1 - which]; a.plo_out = m->plo[1 - which]; a.v_out = m->vel[1 - which];
+  a.w_out = m->angv[1 - which];
+  a.pos = b.pos; a.vel = b.vel; a.angv = b.angv; a.rad = b.rad; a.pmove = b.pmove;
+  a.nebor = b.nebor; a.num_nebor = b.num_nebor; a.plevel = b.plevel; a.nidx = b.nidx; a.npars = b.npars;
+  a.nneb = b.nneb; a.rec = b.rec; a.brg = b.brg; a.wlist = b.wlist; a.nwall = b.nwall; a.wrec = b.wrec;
+  a.force_out = m->force; a.flag = b.flag; a.err = b.err; a.counters = b.counters; a.cyl = b.cyl;
+  a.n = c->n;
+  a.force_cap = c->s.force_cap;
+  a.off = m->off;
+  a.dt = c->s.prm.dt;
+  a.dtf = (float)c->s.prm.dt;
+  a.move_limit = 0.3 * c->s.prm.SearchGap;
+  a.coarse_tol = m->coarse_tol;
+  a.rfrc = (float)c->s.mat[0].rfrc;
+  a.lqd_vol = (float)c->s.lqd.vol;
+  a.lqd_layer = (float)c->s.lqd.layer;
+  a.lqd_gapmn = (float)c->s.lqd.gapmn;
+  a.lqd_st = (float)c->s.lqd.stension;
+  a.pp = make_law(c->s.cal, true, c->s.mat[0].dmpn * c->s.mat[0].dmpn, c->s.load_stage);
+  calParaPP pw;
+  std::memcpy(&pw, &c->s.pwcal, sizeof(pw));
+  a.pw = make_law(pw, false, c->s.mat[0].dmpn * c->s.mat[1].dmpn, c->s.load_stage);
+  const int bs = 128;
+  if (c->s.force_cap == 1)
+    k_step_mixed<true><<<grid_for(c->n, bs), bs, 0, s>>>(a);
+  else
+    k_step_mixed<false><<<grid_for(c->n, bs), bs, 0, s>>>(a);
+  return cuda_check(cudaGetLastError(), "mixed_step launch");
+}
+
+dem_status mixed_pre_rebuild(dem_ctx* c, int which, cudaStream_t s) {
+  /* the bridge counts of the last step travel in the shadow the next step
+   * reads; bring them to the master array before it is permuted */
+  k_lqd_from_shadow<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, c->mx->vel[which], c->b.lqd);
+  return cuda_check(cudaGetLastError(), "mixed_pre_rebuild launch");
+}
+
+dem_status mixed_force_to_master(dem_ctx* c, cudaStream_t s) {
+  k_force_out<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, c->mx->force, c->b.force, c->b.mom);
+  /* the bridge counts of the last step live in the shadow the next step reads */
+  k_lqd_from_shadow<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, c->mx->vel[c->parity], c->b.lqd);
+  return cuda_check(cudaGetLastError(), "mixed_force_to_master launch");
+}
+
+}  // namespace dem

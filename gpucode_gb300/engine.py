@@ -1,0 +1,143 @@
+"""Python handle on the native engine (dem_* C API of libdem_gb300).
+
+Thin: every call goes straight to the C ABI; arrays cross as raw pointers to
+NumPy buffers.  Units are the reference's reduced units on the device side.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import DemInput, DemOptions, DemSetup, DemStats, check, ptr
+
+
+@dataclass
+class Setup:
+    """A derived set-up: dem_setup plus the per-particle radius (reduced),
+    size level and level rank (the reference's Nebor_Idx)."""
+
+    s: DemSetup
+    rad: np.ndarray
+    plevel: np.ndarray
+    nidx: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return int(self.s.np)
+
+    @classmethod
+    def build(cls, inp: DemInput, dia_m: np.ndarray) -> "Setup":
+        lib = _abi.load()
+        dia = np.ascontiguousarray(dia_m, dtype=np.float64)
+        n = int(inp.np)
+        if dia.shape != (n,):
+            raise ValueError(f"diameters: expected shape ({n},), got {dia.shape}")
+        s = DemSetup()
+        rad = np.zeros(n, np.float64)
+        plevel = np.zeros(n, np.int32)
+        nidx = np.zeros(n, np.int32)
+        check(lib.dem_build_setup(C.byref(inp), ptr(dia), C.byref(s), ptr(rad), ptr(plevel), ptr(nidx)),
+              "dem_build_setup")
+        return cls(s, rad, plevel, nidx)
+
+    @classmethod
+    def from_files(cls, genfile: str) -> "Setup":
+        """heyi.in-style keyword file (+ <genfile>_dia.dat) -> set-up."""
+        lib = _abi.load()
+        inp = DemInput()
+        check(lib.dem_read_input(genfile.encode(), C.byref(inp), None), "dem_read_input")
+        dia = np.zeros(inp.np, np.float64)
+        check(lib.dem_read_input(genfile.encode(), C.byref(inp), ptr(dia)), "dem_read_input")
+        return cls.build(inp, dia)
+
+    def to_reduced(self, x_m: np.ndarray) -> np.ndarray:
+        """SI lengths -> reduced lengths (divide by REALSIZE, UnitReduce.cpp:14)."""
+        return np.asarray(x_m, np.float64) / self.s.unit.rlunit
+
+
+class Engine:
+    """One simulation on one GPU (dem_ctx)."""
+
+    def __init__(self, setup: Setup, precision: str = "mixed", reorder: bool = True, use_graph: bool = True,
+                 capillary: str = "formula"):
+        self.lib = _abi.load()
+        self.setup = setup
+        opt = DemOptions()
+        self.lib.dem_default_options(C.byref(opt))
+        opt.precision = {"mixed": _abi.PREC_MIXED, "fp64": _abi.PREC_FP64}[precision]
+        opt.capillary = {"formula": _abi.CAP_FORMULA, "mlp": _abi.CAP_MLP}[capillary]
+        opt.reorder = 1 if reorder else 0
+        opt.use_graph = 1 if use_graph else 0
+        self.opt = opt
+        h = C.c_void_p()
+        check(self.lib.dem_create(C.byref(setup.s), ptr(setup.rad), ptr(setup.plevel), ptr(setup.nidx),
+                                  C.byref(opt), C.byref(h)), "dem_create")
+        self.h = h
+        self.n = setup.n
+
+    # ---- state ----
+    def set_state(self, pos: np.ndarray, vel: np.ndarray | None = None, angvel: np.ndarray | None = None) -> None:
+        p = np.ascontiguousarray(pos, np.float64).reshape(self.n, 3)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float64).reshape(self.n, 3)
+        w = None if angvel is None else np.ascontiguousarray(angvel, np.float64).reshape(self.n, 3)
+        check(self.lib.dem_set_state(self.h, ptr(p), None if v is None else ptr(v), None if w is None else ptr(w)),
+              "dem_set_state")
+
+    def get_state(self) -> dict[str, np.ndarray]:
+        out = {k: np.zeros((self.n, 3), np.float64) for k in ("pos", "vel", "angvel", "force", "mom")}
+        check(self.lib.dem_get_state(self.h, ptr(out["pos"]), ptr(out["vel"]), ptr(out["angvel"]),
+                                     ptr(out["force"]), ptr(out["mom"])), "dem_get_state")
+        return out
+
+    def step(self, nsteps: int = 1) -> None:
+        check(self.lib.dem_step(self.h, int(nsteps)), "dem_step")
+
+    def sync(self) -> None:
+        check(self.lib.dem_sync(self.h), "dem_sync")
+
+    def stats(self) -> dict[str, float]:
+        st = DemStats()
+        check(self.lib.dem_get_stats(self.h, C.byref(st)), "dem_get_stats")
+        return {k: getattr(st, k) for k, _ in DemStats._fields_ if k != "pad"}
+
+    def stream(self) -> int:
+        return int(self.lib.dem_stream(self.h) or 0)
+
+    def neighbors(self, max_per: int = 256) -> tuple[np.ndarray, np.ndarray]:
+        counts = np.zeros(self.n, np.int32)
+        partners = np.full((self.n, max_per), -1, np.int32)
+        check(self.lib.dem_get_neighbors(self.h, ptr(counts), ptr(partners), max_per), "dem_get_neighbors")
+        return counts, partners
+
+    def history(self, max_per: int = 256) -> tuple[np.ndarray, np.ndarray]:
+        rec = np.zeros((self.n, max_per, 8), np.float64)
+        brg = np.zeros((self.n, max_per), np.int32)
+        check(self.lib.dem_get_history(self.h, ptr(rec), ptr(brg), max_per), "dem_get_history")
+        return rec, brg
+
+    def save(self, path: str | os.PathLike, nbatch: int = 1) -> None:
+        check(self.lib.dem_save(self.h, str(path).encode(), nbatch), "dem_save")
+
+    def load(self, path: str | os.PathLike) -> None:
+        check(self.lib.dem_load(self.h, str(path).encode()), "dem_load")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.dem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

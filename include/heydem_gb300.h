@@ -1,0 +1,339 @@
+/*
+ * heydem_gb300.h -- public C ABI of libdem_gb300 (GB300 / sm_103a DEM packing engine).
+ *
+ * Two layers, both plain C (extern "C", raw pointers and sizes, no torch types):
+ *
+ *  1. The reference heyDEM interface, symbol for symbol.  Every function the
+ *     reference declares in heydem.h:366-613 (set-up, constant upload, the
+ *     per-step GPU wrappers, host I/O) is exported here with the identical
+ *     signature and argument meaning, so the reference's driver (main.cpp) links
+ *     against libdem_gb300 unchanged.  Each declaration cites the reference
+ *     line it replaces.  These entry points keep the reference's data layouts
+ *     (double3 AoS particle arrays, level/slot-major neighbour slots,
+ *     slot-major contact history, pitched wall list) and run this library's
+ *     own sm_103a kernels on them, on the legacy default stream, in FP64 with
+ *     the reference's formulas.  Like the reference they return void; a CUDA
+ *     failure prints the error and exits (heydem.h:25-35 behaviour), and
+ *     dem_last_error() reports the most recent failure for callers that do not
+ *     want to exit.
+ *
+ *  2. The native dem_* interface: a context that owns cell-sorted SoA device
+ *     state, runs whole time steps as one CUDA graph (rebuild decided on the
+ *     device), supports an FP32-force / FP64-state mode, returns status codes
+ *     and imports/exports the reference's double3 host arrays at feed and output
+ *     points.
+ *
+ * Units: everything on the device is in the reference's reduced units
+ * (UnitReduce.cpp:14-20: length = REALSIZE, the largest diameter; mass =
+ * rho*pi*D^3/6; force = m*g; time = sqrt(D/g)).
+ */
+#ifndef HEYDEM_GB300_H
+#define HEYDEM_GB300_H
+
+#include <stddef.h>
+#include <stdio.h>
+#include <vector_types.h> /* double2, double3, int3: layout of the reference's structs */
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Reference data model (heydem.h:39-320), layout-identical                   */
+/* ------------------------------------------------------------------------ */
+#ifndef HEYI_COMMON_H /* the reference's own heydem.h already declared these */
+#define DEM_NUM_MAT 2 /* heydem.h:14 NUM_MAT */
+
+typedef struct CylinderBC { double2 cir; double R; double Tw; double Bw; double topv, btmv; } CylinderBC; /* heydem.h:39-46 */
+typedef struct FeedZone { double Lmax; double Lmin; } FeedZone;                                      /* heydem.h:63-67 */
+typedef struct UNIT { double rlunit, rmunit, rfunit; double reunit, rsunit, rtunit, rvunit; } UNIT;   /* heydem.h:81-85 */
+typedef struct MatType { double density; double emod, ymod, pois; double dmpn; double sfrc, rfrc; double yldp; } MatType; /* heydem.h:90-97 */
+typedef struct LIQUID { double stension; double vol; double gapmn; double layer; double brknmx; } LIQUID; /* heydem.h:104-111 */
+typedef struct SIMULATION {                                                                          /* heydem.h:118-135 */
+  double dt, dtFactor, cutGap, ctime, simTime, fdtime, outtime, dumptime, outinterval, fdinterval;
+  int iter; int Outs;
+} SIMULATION;
+typedef struct LOADMODE { int stage; double tPacking; int nOutPacking; } LOADMODE;                   /* heydem.h:142-148 */
+typedef struct PPCONTACT_HISTORY {                                                                   /* heydem.h:153-173 */
+  double3 *dispt; double3 *ShrForB; double3 *ShrMomB; double3 *nOld;
+  double *nDsp; double *nDsp_mx; double *plstRad; double *plstDfm; double *bndRad;
+  double *NorForB; double *NorMomB; double *TenStrn; double *ShrStrn;
+  int *stage; int *lqdBrg; int *Exbond;
+} PPCONTACT_HISTORY;
+typedef struct PWCONTACT_HISTORY {                                                                   /* heydem.h:179-190 */
+  double3 *dispt; double *nDsp; double *nDsp_mx; double *plstRad; double *plstDfm; int *stage; int *lqdBrg;
+} PWCONTACT_HISTORY;
+typedef struct PARAMETER { double3 Origin; double3 EndPoint; double SearchGap; double dt; int NP; } PARAMETER; /* heydem.h:196-204 */
+typedef struct SEARCHCELL { int *numCells; int3 *gridSize; double *Cellsize; } SEARCHCELL;        /* heydem.h:209-214 */
+typedef struct calParaPP { double emod, pois, sfrc, ystress, ydsp_t, yforce_t, ystiff_t; } calParaPP; /* heydem.h:220-229 */
+typedef struct calParaPW { double emod, pois, sfrc, ystress, ydsp_t, yforce_t, ystiff_t; } calParaPW; /* heydem.h:233-242 */
+#endif /* HEYI_COMMON_H */
+
+/* ------------------------------------------------------------------------ */
+/* Layer 1: the reference's extern "C" API (heydem.h:366-613)                 */
+/* ------------------------------------------------------------------------ */
+
+/* Process-global particle arrays the reference driver touches directly
+ * (Allocation.cpp:5-18, declared in heydem.h:329-347).  C++ linkage, as in the
+ * reference; defined by libdem_gb300 and filled by ParticleInfoAlloc /
+ * SearchCellAlloc. */
+#ifdef __cplusplus
+}
+extern double3 *hPos, *hVel, *hAngVel, *hForce;
+extern double* hRad;
+extern double3 *dPos, *dVel, *dAngVel, *dForce, *dMom;
+extern double *dRMom, *dRad;
+extern int *d_GridParticleHash, *d_GridParticleIndex, *d_CellStart, *d_CellEnd;
+extern "C" {
+#endif
+
+/* set-up and allocation */
+void ParticleInfoAlloc(int NP);                                                                    /* heydem.h:366 */
+void PPCntHstry_Alloc(PPCONTACT_HISTORY* h_cntHstry_pp, PPCONTACT_HISTORY* d_cntHstry_pp,
+                      PPCONTACT_HISTORY* d_cntHstry_ppOld, int nPPCnt);                            /* heydem.h:369 (C++ refs = pointers) */
+void WallCntHstry_Alloc(PWCONTACT_HISTORY* h_cntHstry_Stlpw, PWCONTACT_HISTORY* d_cntHstry_Stlpw,
+                        PWCONTACT_HISTORY* d_cntHstry_Stlpw_Old, int nWallCnt);                    /* heydem.h:372 */
+void NeborListAlloc(int** h_Num_Nebor, int** h_1DNebor, double** d_pMoveforReBld, int** d_Num_Nebor,
+                    int** d_Num_Nebor_Old, int** d_Nebor1, int** d_Nebor1_Old, int** h_Num_stlWall,
+                    int** h_StlWList_1D, int** d_Num_StlWall, int** d_Num_StlWall_Old,
+                    int** d_StlW_List, int** d_StlW_List_Old, size_t* pitch_Sw1, size_t* pitch_Sw2,
+                    int NP, int nPPCnt, int StlMaxWallPerBall);                                    /* heydem.h:375 */
+void VarInit(double3** dForce, double3** dMom, double** dRMom, int** d_lqdCnt, int** d_lqdCnt_Old,
+             int NP);                                                                              /* heydem.h:386 */
+void FeedZoneAlloc(FeedZone** Feedcube);                                                           /* heydem.h:393 */
+void ParamAlloc(SIMULATION** h_dem, UNIT** Rdu, int** h_lqdCnt, int** d_lqdCnt, int** d_lqdCnt_Old,
+                MatType** h_Mat, LIQUID** h_lqd, PARAMETER** h_Params, SEARCHCELL* h_cell,
+                SEARCHCELL* d_cell, int nLevels, int NP);                                          /* heydem.h:396 */
+void SearchCellAlloc(int NP, int numCells);                                                        /* heydem.h:402 */
+
+/* host input / output (keyword file heyi.in, diameters, dump header, Tecplot) */
+void FindRec(FILE* inFile, char* strDest);                                                         /* heydem.h:407 */
+void ReadData(double* h_Level_size, int* h_pLevel, int* h_level_nNebors, int* h_level_nPars,
+              int* h_Nebor_Idx, CylinderBC** h_Cir, CylinderBC** d_Cir, FeedZone* Feedcube,
+              MatType* h_Mat, LIQUID* h_lqd, PARAMETER* h_Params, double* InitParSize,
+              int* ForceCap, SIMULATION* h_dem, LOADMODE* h_load, double* hRad, SEARCHCELL h_cell,
+              int NP, int nLevels, char* genfile, int RESTART);                                   /* heydem.h:410 */
+void LoadPara(char* DumpName, int* NP, int* nBatch, int* TotalParticle);                           /* heydem.h:418 */
+void WrtTec(double3* hPos, double3* hVel, double3* hForce, double3* hAngVel, SIMULATION* h_dem,
+            double* hRad, UNIT* Rdu, int TotalParticle, int NP);                                   /* heydem.h:422 */
+void DiaInput(char* diaFile, double* hRad, int NP);                                                /* heydem.h:427 */
+void UnitReduce(UNIT* Rdu, CylinderBC* h_Cir, FeedZone* Feedcube, LOADMODE* h_load, double* hRad,
+                MatType* h_Mat, LIQUID* h_lqd, double InitParSize, SIMULATION* h_dem,
+                PARAMETER* h_Params, SEARCHCELL h_cell, double* h_Level_size, int nLevels, int NP,
+                int RESTART, char* genfile);                                                       /* heydem.h:432 */
+int ParticleFeed(FeedZone* Feedcube, CylinderBC* h_Cir, double InitParSize, double3* hPos,
+                 double* hRad, int numParticle, int NP);                                           /* heydem.h:440 */
+
+/* constant upload (kernel.cu:22-50) */
+void setMaterial(MatType* h_Mat);                                                                  /* heydem.h:453 */
+void setLiquid(LIQUID* h_lqd);                                                                     /* heydem.h:454 */
+void setParameters(PARAMETER* h_Params);                                                           /* heydem.h:455 */
+void setCalpara(calParaPP* h_cal, calParaPW* h_pWcal);                                             /* heydem.h:456 */
+void IndexOffset(int* d_Num, int* d_nei, int Nn);                                                  /* heydem.h:457 */
+
+/* per-step GPU wrappers (ParticleSystem.cu:141-375) */
+void BldNeborList(int* d_GridParticleHash, int* d_GridParticleIndex, int* d_CellStart,
+                  int* d_CellEnd, int* d_pLevel, SEARCHCELL d_cell, int* d_Ncell_Idx,
+                  double* d_Level_size, int* d_level_nPars, int* d_level_nNebors, int nLevels,
+                  double3* dPos, int Sys_nCells, int* d_Nebor1, int* d_Nebor_Idx, int* d_Num_Nebor,
+                  int TotalParticle, double* dRad);                                                /* heydem.h:547 */
+void BldCirWall(double3* dPos, double* dRad, CylinderBC* d_Cir, int* d_StlW_List, size_t pitch_Sw1,
+                int* d_Num_StlWall, int TotalParticle);                                            /* heydem.h:556 */
+void HstryCopy(int* d_Nebor1, int* d_OldNebor1, int* d_pLevel, int* d_level_nNebors,
+               int* d_level_nPars, int* d_Nebor_Idx, PPCONTACT_HISTORY d_cntHstry_ppOld,
+               PPCONTACT_HISTORY d_cntHstry_pp, int* d_Num_Nebor, int* d_Num_Nebor_Old,
+               int TotalParticle, int NP);                                                         /* heydem.h:561 */
+void HstryCopyPW(int* d_StlW_List, int* d_StlW_List_Old, size_t pitch_w1, size_t pitch_w2,
+                 PWCONTACT_HISTORY d_cntHstry_pw_Old, PWCONTACT_HISTORY d_cntHstry_pw,
+                 int* d_Num_StlWall, int* d_Num_StlWall_Old, int TotalParticle, int NP);          /* heydem.h:569 */
+void PpInterCalc(double3* dPos, double3* dVel, double3* dAngVel, double* dRad, int* d_Nebor1,
+                 int* d_pLevel, int* d_level_nNebors, int* d_level_nPars, int* d_Nebor_Idx,
+                 PPCONTACT_HISTORY d_cntHstry_pp, int* d_Num_Nebor, int* d_lqdCnt,
+                 int* d_lqdCnt_Old, double3* dForce, double3* dMom, double* dRMom,
+                 int TotalParticle, int NP, int ForceCap, int stage);                              /* heydem.h:577 */
+void CirPWCalc(double3* dPos, double3* dVel, double3* dAngVel, double3* dForce, double3* dMom,
+               double* dRMom, double* dRad, CylinderBC* d_Cir, PWCONTACT_HISTORY d_cntHstry_Stlpw,
+               int* d_Num_StlWall, int* d_StlW_List, size_t pitch_Sw1, int TotalParticle, int NP,
+               int stage);                                                                         /* heydem.h:590 */
+void UpdateSystem(double* dRad, double3* dPos, double3* dVel, double3* dAngVel, double3* dForce,
+                  double3* dMom, double* dRMom, int* d_ReNebld, double* d_pMoveforReBld,
+                  int TotalParticle);                                                              /* heydem.h:600 */
+void NeborToCPU(int* h_Num_Nebor, int* d_Num_Nebor, int* h_1DNebor, int* d_Nebor1, int* h_Num_stlWall,
+                int* d_Num_StlWall, int* h_StlWList_1D, int* d_StlW_List,
+                PPCONTACT_HISTORY h_cntHstry_pp, PPCONTACT_HISTORY d_cntHstry_pp,
+                PWCONTACT_HISTORY h_cntHstry_Stlpw, PWCONTACT_HISTORY d_cntHstry_Stlpw, int NP,
+                int nPPCnt, size_t pitch_Sw1, int StlMaxWallPerBall);                              /* heydem.h:605 */
+void WallCntHstryCopy(PWCONTACT_HISTORY d_cntHstry_Stlpw_Old, PWCONTACT_HISTORY d_cntHstry_Stlpw,
+                      int nWallCnt);                                                               /* heydem.h:612 */
+void PPCntHstryCopy(PPCONTACT_HISTORY d_cntHstry_ppOld, PPCONTACT_HISTORY d_cntHstry_pp,
+                    int nPPCnt);                                                                   /* heydem.h:613 */
+
+/* Note on C++ reference parameters: heydem.h declares the *_Alloc, VarInit,
+ * ParamAlloc and ReadData pointer arguments as C++ references (T*& / T&).  On
+ * the Itanium C++ ABI a reference is passed exactly as a pointer, so the
+ * pointer forms above are the same machine-level signature and main.cpp's
+ * calls bind to them unchanged. */
+
+/* ------------------------------------------------------------------------ */
+/* Layer 2: native interface                                                 */
+/* ------------------------------------------------------------------------ */
+
+typedef int dem_status;
+enum {
+  DEM_OK = 0,
+  DEM_ERR_ARG = -1,      /* bad argument / size */
+  DEM_ERR_CUDA = -2,     /* a CUDA call failed (see dem_last_error) */
+  DEM_ERR_OVERFLOW = -3, /* a neighbour list ran past its level's slot capacity */
+  DEM_ERR_NONFINITE = -4,/* NaN/Inf in particle state */
+  DEM_ERR_IO = -5,       /* file missing / keyword missing / parse error */
+  DEM_ERR_STATE = -6,    /* call out of order */
+  DEM_ERR_NOMEM = -7,    /* device allocation failed */
+  DEM_ERR_CELL = -8      /* a particle left the cell grid */
+};
+
+#define DEM_MAX_LEVELS 16
+
+/* What heyi.in holds (ReadData.cpp:75-187, main.cpp:63-84), in SI units. */
+typedef struct dem_input {
+  int np;                 /* NUMPARTICLE */
+  int n_levels;           /* SIZELEVEL */
+  int load_stage;         /* LOADMODE */
+  double t_packing;       /* packing_TIME [s] */
+  int force_cap;          /* FoceCapillary yes/no */
+  double real_size;       /* REALSIZE [m]: the largest diameter, the length unit */
+  double cut_gap;         /* CUTGAPFORNEIGHBORLIST (in units of REALSIZE*Rmax/Rmin) */
+  double expand_size;     /* EXPANDSIZE (domain margin in units of Rmax) */
+  double cyl_x, cyl_y, cyl_bw, cyl_r, cyl_h; /* CylinderBC x y Bw R H [m] */
+  double feed_lmin, feed_lmax;               /* FeedZone [m] */
+  double mat[2][7];       /* MATERIAL: density ymod pois sfrc rfrc dmpn yldp, particle then wall */
+  double lqd[3];          /* LIQUID: stension vol gapmn */
+  double dt_factor;       /* SIMULATION dtFactor */
+  int n_out;              /* SIMULATION nOut */
+  int level_input;        /* SIZELEVEL_INPUT yes/no */
+  double level_dia[DEM_MAX_LEVELS]; /* SIZELEVEL_INPUT diameters [m] */
+  double dt_override;     /* > 0: use this dt [s] instead of the dtFactor rule (ReadData.cpp:263) */
+  double gravity;         /* 0: the reference's 9.8 (heydem.h:16) */
+} dem_input;
+
+/* Everything the step path needs, derived exactly as ReadData.cpp:243-375,
+ * UnitReduce.cpp:14-104 and main.cpp:328-348 derive it (reduced units). */
+typedef struct dem_setup {
+  int np, n_levels, force_cap, load_stage;
+  double init_par_size;   /* REALSIZE [m] */
+  CylinderBC cyl;
+  FeedZone feed;
+  MatType mat[2];
+  LIQUID lqd;
+  PARAMETER prm;
+  calParaPP cal;
+  calParaPW pwcal;
+  UNIT unit;
+  SIMULATION sim;
+  LOADMODE load;
+  double level_size[DEM_MAX_LEVELS];
+  int level_nnebors[DEM_MAX_LEVELS];
+  int level_npars[DEM_MAX_LEVELS];
+  double cell_size[DEM_MAX_LEVELS];
+  int3 grid_size[DEM_MAX_LEVELS];
+  int num_cells[DEM_MAX_LEVELS];
+  int ncell_idx[DEM_MAX_LEVELS]; /* inclusive scan of num_cells (IndexOffset) */
+  int sys_ncells;
+  long long n_pp_slots;           /* nPPCnt = sum level_npars * level_nnebors */
+  double rad_min, rad_max;        /* reduced */
+} dem_setup;
+
+/* heyi.in (+ <genfile>_dia.dat when present) -> dem_input + diameters [m].
+ * dia must hold np doubles; pass NULL to query np/n_levels only. */
+dem_status dem_read_input(const char* genfile, dem_input* in, double* dia);
+/* dem_input + diameters [m] -> dem_setup + per-particle rad (reduced), level and
+ * level rank (Nebor_Idx). */
+dem_status dem_build_setup(const dem_input* in, const double* dia, dem_setup* out, double* rad,
+                           int* plevel, int* nebor_idx);
+
+/* precision of the native step */
+enum { DEM_PREC_FP64 = 0, DEM_PREC_MIXED = 1 };
+/* capillary closure */
+enum { DEM_CAP_FORMULA = 0, DEM_CAP_MLP = 1 };
+
+typedef struct dem_options {
+  int precision;          /* DEM_PREC_* */
+  int capillary;          /* DEM_CAP_* */
+  int block_size;         /* threads per block of the step kernel (0 = default) */
+  int reorder;            /* 1: keep particles in cell order (default); 0: reference order */
+  int use_graph;          /* 1: replay steps through a CUDA graph (default) */
+  int seed;               /* reserved */
+} dem_options;
+
+typedef struct dem_ctx dem_ctx;
+
+typedef struct dem_stats {
+  long long iter;         /* steps taken */
+  long long rebuilds;     /* neighbour-list rebuilds */
+  long long nb_entries;   /* neighbour-list entries at the last rebuild */
+  long long contacts;     /* directed p-p contacts (gap < 0) in the last step */
+  long long bridges;      /* directed wet non-contact bridges in the last step */
+  long long wall_contacts;/* particle-wall contacts in the last step */
+  int error_bits;         /* device error word (1: overflow, 2: non-finite, 4: cell range) */
+  int pad;
+  double ctime;           /* simulated time (reduced) */
+} dem_stats;
+
+void dem_default_options(dem_options* o);
+dem_status dem_create(const dem_setup* s, const double* rad, const int* plevel,
+                      const int* nebor_idx, const dem_options* opt, dem_ctx** out);
+dem_status dem_destroy(dem_ctx* c);
+/* Host state in the reference's double3 layout and particle order (reduced
+ * units).  vel/angvel may be NULL (zero).  Marks the lists for rebuild. */
+dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel);
+/* Any pointer may be NULL.  force/mom are the last step's totals. */
+dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,
+                         double3* mom);
+/* Advance nsteps time steps.  Device-resident; no host synchronisation inside
+ * unless the context was created without graphs. */
+dem_status dem_step(dem_ctx* c, int nsteps);
+/* Wait for the context's stream and check the device error word. */
+dem_status dem_sync(dem_ctx* c);
+dem_status dem_get_stats(dem_ctx* c, dem_stats* st);
+/* The context's CUDA stream (cudaStream_t) for callers that time or order work. */
+void* dem_stream(dem_ctx* c);
+/* Current neighbour lists in the reference's terms: for every particle i (in
+ * the caller's order) its partners (caller's ids) in the reference's list order.
+ * counts[np]; partners[np*max_per] (row i = partners of i).  Returns
+ * DEM_ERR_ARG if max_per is too small. */
+dem_status dem_get_neighbors(dem_ctx* c, int* counts, int* partners, int max_per);
+/* Contact history of the pair (i, partners[i][k]) in reference terms,
+ * rec[np*max_per][8] = dispt.x dispt.y dispt.z nDsp nDsp_mx plstRad plstDfm
+ * stage, plus bridge flags brg[np*max_per]. */
+dem_status dem_get_history(dem_ctx* c, double* rec, int* brg, int max_per);
+/* Write / read the full engine state (binary, with the reference's
+ * "SYSTEM Info" text header so LoadPara can parse it). */
+dem_status dem_save(dem_ctx* c, const char* path, int nBatch);
+dem_status dem_load(dem_ctx* c, const char* path);
+
+/* Seed of ParticleFeed's generator (the reference seeds from the clock,
+ * ParticleFeed.cpp:17; here feeds are reproducible). */
+void dem_set_feed_seed(unsigned long long seed);
+/* Reads and clears the error word of the reference-compatible entry points:
+ * bit 1 = a neighbour list stopped at its level's slot capacity (the
+ * reference would write past it, kernel.cu:833-836), bit 4 = a particle hashed
+ * outside the cell grid. */
+int dem_compat_errors(void);
+/* Seeded sequential deposition into a cylinder (test / benchmark inputs):
+ * particles in the given order are dropped at the lowest of `tries` random
+ * (x, y) candidates inside radius R - r of the axis (cx, cy) onto the floor z0
+ * or the highest sphere below them, with a clearance `gap` between surfaces.
+ * dia[n] and pos_out[n] in the same (any) length unit. */
+dem_status dem_pack_deposit(int n, const double* dia, double cx, double cy, double R, double z0,
+                            double gap, int tries, unsigned long long seed, double3* pos_out);
+/* Struct sizes and offsets of this header, for binding checks. */
+int dem_abi_layout(long long* out, int cap);
+
+/* Most recent error message (thread-local), never NULL. */
+const char* dem_last_error(void);
+/* Library build string. */
+const char* dem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HEYDEM_GB300_H */
