@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Benchmark: particle-steps/s of the wet polydisperse packing (200,000 spheres)
+on one GB300, FP32-force / FP64-state path.
+
+One bench "step" is one DEM time step of the whole bed (rebuild when flagged,
+p-p contact + capillary, wall contact, integration), replayed from a one-step
+CUDA graph whose rebuild decision is taken on the device.  The working set of a
+step (~90 MB) fits in the 129 MB L2, so L2 is evicted between timed steps (a
+256 MB write followed by a 256 MB read on the same stream, outside the per-step
+CUDA events, so the step starts cold and pays no write-backs of the eviction).
+Before timing, the deposited bed settles under gravity for --settle steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (launched by torchrun) every rank runs its own replica of the bed:
+the path does not shard across GPUs here (replicas only); value sums all ranks'
+particle-steps over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s, 200k wet spheres, vs FP64 plain; packing-frac & Z error"
+UNIT = "particle-steps/s"
+
+
+def _peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self, gpu_index: int = 0) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9 or f[0] != str(gpu_index):
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def cpu_oracle_rate(w, pos, steps: int, threads: int) -> tuple[float, str]:
+    """The FP64 oracle (reference algorithm on the host cores, OpenMP) on the same bed."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    if not pyoracle.ORACLE_LIB.exists():
+        pyoracle.build_oracle()
+    sim = pyoracle.OracleSim(w.setup, pos)
+    sim.step(1)  # first neighbour build, untimed
+    t0 = time.perf_counter()
+    sim.step(steps)
+    dt = time.perf_counter() - t0
+    sim.close()
+    return w.setup.n * steps / dt, f"{steps} steps of the {w.setup.n}-sphere bed after its first list build"
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from gpucode_gb300 import configs
+
+    w = configs.wet()
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    if not pyoracle.ORACLE_LIB.exists():
+        pyoracle.build_oracle()
+    sim = pyoracle.OracleSim(w.setup, w.pos0_reduced)
+    sim.step(1 + args.warmup)
+    t0 = time.perf_counter()
+    sim.step(args.steps)
+    dt = time.perf_counter() - t0
+    val = w.setup.n * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded deposited bed, log-normal sizes)",
+        "config": {"workload": "wet200k", "particles": w.setup.n, "dt_s": 5e-7, "levels": int(w.setup.s.n_levels)},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} steps of the full bed on the host cores (FP64 oracle restating "
+                                   "the reference kernels; the reference sources are not on this host)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def traffic_from_profiles() -> float | None:
+    """DRAM bytes per launch of the fused step kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "step_mixed_wet200k.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--profile-reps", type=int, default=20)
+    ap.add_argument("--settle", type=int, default=2000,
+                    help="untimed steps before the warm-up: gravity loads the deposited bed's contacts")
+    ap.add_argument("--host-steps", action="store_true",
+                    help="launch every step's kernels directly instead of from CUDA graphs (for ncu, which "
+                         "cannot profile kernels of graphs with conditional nodes)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank = _dist()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+
+    from gpucode_gb300 import configs
+    from gpucode_gb300.engine import Engine
+
+    w = configs.wet()
+    n = w.setup.n
+    import ctypes as C
+
+    from gpucode_gb300._abi import check, ptr
+
+    eng = Engine(w.setup, precision="mixed", use_graph=not args.host_steps, graph_steps=1)
+    eng.set_state(w.pos0_reduced)
+    stream = torch.cuda.ExternalStream(eng.stream())
+    # L2 eviction between timed steps: write 256 MB, then read another 256 MB,
+    # so each step starts with a cold L2 holding clean, unrelated lines
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    eng.lib.dem_l2_flush.restype = C.c_int
+    eng.lib.dem_l2_flush.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+
+    def l2_flush():
+        check(eng.lib.dem_l2_flush(C.c_void_p(eng.stream()), C.c_void_p(flush.data_ptr()), flush.numel()),
+              "dem_l2_flush")
+
+    eng.step(args.settle)
+    eng.step(args.warmup)
+    eng.sync()
+    s0 = eng.stats()
+    clocks = Clocks()
+    clocks.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    evs = []
+    for _ in range(args.steps):
+        l2_flush()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.step(1)
+        b.record(stream)
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    t_wall = time.perf_counter() - t_wall
+    ck = clocks.stop(local)
+    eng.sync()
+    s1 = eng.stats()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    steps = args.steps
+    value = ws * n * steps / (ms / 1000.0)
+
+    # measured pair counts per particle-step over the timed region
+    d = {k: s1[k] - s0[k] for k in ("nb_entries", "contacts", "bridges", "wall_contacts", "rebuilds")}
+    ps = n * steps
+    n_nb, n_c, n_w, n_wall = d["nb_entries"] / ps, d["contacts"] / ps, d["bridges"] / ps, d["wall_contacts"] / ps
+    bytes_per_particle = 152 + 4 * n_nb + 128 * n_c + 16 * n_w + 128 * n_wall
+
+    # the fused step kernel alone, cold L2 per launch
+    ms_k = C.c_double()
+    check(eng.lib.dem_profile_step(eng.h, args.profile_reps, C.c_void_p(flush.data_ptr()), flush.numel(),
+                                   C.byref(ms_k)), "dem_profile_step")
+    peak, peak_kind = _peaks()
+    achieved = n * bytes_per_particle / (ms_k.value * 1e-3) / 1e9
+    traffic = traffic_from_profiles()
+
+    # end to end through the public API with host buffers: H2D state, one step, D2H state + force
+    hp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hv = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hw = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hf = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    check(eng.lib.dem_get_state(eng.h, ptr(hp), ptr(hv), ptr(hw), None, None), "dem_get_state")
+    E = args.e2e_steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(E):
+        check(eng.lib.dem_set_state_ex(eng.h, ptr(hp), ptr(hv), ptr(hw), 0), "dem_set_state_ex")
+        check(eng.lib.dem_step(eng.h, 1), "dem_step")
+        check(eng.lib.dem_get_state(eng.h, ptr(hp), ptr(hv), ptr(hw), ptr(hf), None), "dem_get_state")
+    e2e_t = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_t], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e = ws * n * E / e2e_t
+    eng.sync()
+
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        if args.cpu_steps > 0:
+            cpu_val, cpu_sample = cpu_oracle_rate(w, w.pos0_reduced, args.cpu_steps, threads)
+        else:
+            cpu_val, cpu_sample = None, "skipped (--cpu-steps 0)"
+        launches_per_step = 2  # decide + fused step kernel
+        rebuild_launches = 15  # lqd copy, copy_old, zero, hash, 3 scan, scatter, order, permute, copy_back,
+        #                        neighbour, wall list, carry, shadows
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-force/f64-state", "data": "synthetic (seeded deposited bed, log-normal sizes)",
+            "config": {"workload": "wet200k", "particles": n, "levels": int(w.setup.s.n_levels), "dt_s": 5e-7,
+                       "capillary": "formula", "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "evicted between timed steps (256 MB write + 256 MB read, outside the per-step events)",
+                       "per_step_counts": {"n_nb": n_nb, "n_c": n_c, "n_w": n_w, "n_wall": n_wall,
+                                           "rebuilds": d["rebuilds"]},
+                       "wall_s": t_wall},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_step_mixed (fused contact + capillary + wall + integrate)",
+                         "bytes_per_particle": bytes_per_particle, "kernel_ms": ms_k.value},
+            "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": cpu_sample},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * 72, "d2h_bytes_per_step": n * 96},
+            "gpu_launches": launches_per_step * steps + rebuild_launches * d["rebuilds"],
+            "clocks": ck,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

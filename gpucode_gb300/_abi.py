@@ -121,7 +121,7 @@ class DemSetup(C.Structure):
 
 class DemOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("capillary", C.c_int), ("block_size", C.c_int), ("reorder", C.c_int),
-                ("use_graph", C.c_int), ("seed", C.c_int)]
+                ("use_graph", C.c_int), ("graph_steps", C.c_int)]
 
 
 class DemStats(C.Structure):
@@ -184,6 +184,8 @@ def _declare(lib: C.CDLL) -> None:
         "dem_create": (I, [C.POINTER(DemSetup), P, P, P, C.POINTER(DemOptions), C.POINTER(P)]),
         "dem_destroy": (I, [P]),
         "dem_set_state": (I, [P, P, P, P]),
+        "dem_set_state_ex": (I, [P, P, P, P, I]),
+        "dem_profile_step": (I, [P, I, P, C.c_size_t, C.POINTER(C.c_double)]),
         "dem_get_state": (I, [P, P, P, P, P, P]),
         "dem_step": (I, [P, I]),
         "dem_sync": (I, [P]),
@@ -191,6 +193,7 @@ def _declare(lib: C.CDLL) -> None:
         "dem_stream": (P, [P]),
         "dem_get_neighbors": (I, [P, P, P, I]),
         "dem_get_history": (I, [P, P, P, I]),
+        "dem_get_aux": (I, [P, P, P, P, P, P, P]),
         "dem_save": (I, [P, C.c_char_p, I]),
         "dem_load": (I, [P, C.c_char_p]),
         "dem_set_feed_seed": (None, [C.c_ulonglong]),

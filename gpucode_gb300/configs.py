@@ -9,7 +9,11 @@ positions) for the packing workloads:
              skin 0.1 d, no liquid.
   wet200k -- 200,000 log-normal spheres (median 1 mm, sigma_ln 0.2, resampled
              into [0.5, 2] mm), cylinder R = 25 mm, capillary bridges on,
-             dt = 5e-7 s, four size levels, seeded deposition start.
+             dt = 5e-7 s, four size levels.  Start: a seeded sequential
+             deposition (each sphere dropped at the lowest of 8 random spots
+             onto the floor or the spheres below, touching, no overlaps), i.e.
+             a loose bed raining into the cylinder; the 25 ms the workload
+             simulates is too short for a dilute lattice to pack.
 
 Parameter mapping onto the reference's knobs (it has no restitution or yield
 overlap inputs):
@@ -257,14 +261,14 @@ def dry(n: int = 5000, cyl_r: float = 8e-3, seed: int = 1, steps: int = 20000, d
 
 def wet(n: int = 200_000, cyl_r: float = 25e-3, seed: int = 2, steps: int = 50000, dt: float = 5e-7,
         n_levels: int = 4, skin_d: float = 1e-4, bridge_frac: float = 0.0125, gravity: float = 0.0,
-        deposit_tries: int = 4) -> Workload:
+        deposit_tries: int = 8) -> Workload:
     """Wet polydisperse packing: log-normal sizes, capillary bridges, deposited bed."""
     dia = lognormal_diameters(n, 1e-3, 0.2, 0.5e-3, 2.0e-3, seed)
     real = 2.0e-3  # REALSIZE: the largest admissible diameter
     rmin, rmax = dia.min() / 2, dia.max() / 2
     yldp = yldp_for_yield_overlap(0.01, E_YOUNG, NU)
     dmpn = calibrate_dmpn(0.7, 0.5, 1e-3, RHO, E_YOUNG, NU, yldp)
-    pos = deposit(dia, cyl_r, 0.0, 0.02e-3, deposit_tries, seed)
+    pos = deposit(dia, cyl_r, 0.0, 0.0, deposit_tries, seed)
     top = float((pos[:, 2] + dia / 2).max())
     cut_gap = (skin_d / real) * rmax / rmin
     inp = make_input(n, n_levels, real, cut_gap, cyl_r, top + 10 * real, RHO, E_YOUNG, NU, MU, dmpn, yldp, 1,

@@ -304,14 +304,15 @@ dem_status enqueue_step(dem_ctx* c, cudaStream_t s, int parity) {
 }
 
 void destroy_graph(dem_ctx* c) {
-  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-  c->graph_exec = nullptr;
-  c->graph_steps = 0;
+  for (int p = 0; p < 2; p++) {
+    if (c->graph_exec[p]) cudaGraphExecDestroy(c->graph_exec[p]);
+    c->graph_exec[p] = nullptr;
+  }
 }
 
-/* G steps: [decide -> IF(rebuild) -> step] x G, parity alternating from 0 */
-dem_status build_graph(dem_ctx* c, int G) {
-  destroy_graph(c);
+/* G steps: [decide -> IF(rebuild) -> step] x G; the mixed path's shadow
+ * parity alternates from start_parity */
+dem_status build_graph(dem_ctx* c, int G, int start_parity) {
   cudaStream_t cs;
   cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_check(e, "capture stream");
@@ -327,7 +328,7 @@ dem_status build_graph(dem_ctx* c, int G) {
   }
   cudaGraphNode_t prev = nullptr;
   for (int step = 0; step < G && st == DEM_OK; step++) {
-    const int parity = (c->opt.precision == DEM_PREC_MIXED) ? (step & 1) : 0;
+    const int parity = (c->opt.precision == DEM_PREC_MIXED) ? ((start_parity + step) & 1) : 0;
     cudaGraphConditionalHandle h;
     if (!ck(cudaGraphConditionalHandleCreate(&h, g, 0, 0), "conditional handle")) break;
     cudaGraphNode_t nd;
@@ -374,10 +375,7 @@ dem_status build_graph(dem_ctx* c, int G) {
   }
   if (st == DEM_OK) {
     cudaGraphExec_t ex = nullptr;
-    if (ck(cudaGraphInstantiate(&ex, g, 0), "cudaGraphInstantiate")) {
-      c->graph_exec = ex;
-      c->graph_steps = G;
-    }
+    if (ck(cudaGraphInstantiate(&ex, g, 0), "cudaGraphInstantiate")) c->graph_exec[start_parity] = ex;
   }
   cudaGraphDestroy(g);
   cudaStreamDestroy(cs);
@@ -407,7 +405,7 @@ dem_status host_step(dem_ctx* c) {
   return DEM_OK;
 }
 
-constexpr int kGraphSteps = 16;
+int graph_len(const dem_ctx* c) { return c->opt.graph_steps > 0 ? c->opt.graph_steps : 16; }
 
 }  // namespace
 }  // namespace dem
@@ -440,8 +438,7 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   c->n = s->np;
   c->slots = s->n_pp_slots;
   c->mx = nullptr;
-  c->graph_exec = nullptr;
-  c->graph_steps = 0;
+  c->graph_exec[0] = c->graph_exec[1] = nullptr;
   c->parity = 0;
   c->iter = 0;
   c->ctime = 0.0;
@@ -542,6 +539,11 @@ extern "C" dem_status dem_destroy(dem_ctx* c) {
 extern "C" void* dem_stream(dem_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 extern "C" dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel) {
+  return dem_set_state_ex(c, pos, vel, angvel, 1);
+}
+
+extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel,
+                                       int request_rebuild) {
   if (!c || !pos) return fail(DEM_ERR_ARG, "dem_set_state: null argument");
   const size_t N = (size_t)c->n;
   EngineBufs& b = c->b;
@@ -553,9 +555,17 @@ extern "C" dem_status dem_set_state(dem_ctx* c, const double3* pos, const double
   if (e != cudaSuccess) return cuda_check(e, "dem_set_state upload");
   k_import<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_pos, b.tmp_vel, b.tmp_angv, b.pos, b.vel,
                                                          b.angv, vel != nullptr, angvel != nullptr);
-  const int one = 1;
-  e = cudaMemcpyAsync(b.need, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (request_rebuild) {
+    const int one = 1;
+    e = cudaMemcpyAsync(b.need, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_check(e, "dem_set_state");
+  } else if (c->opt.precision == DEM_PREC_MIXED) {
+    /* the neighbours read the shadow copy: refresh it from the new state */
+    dem_status st = mixed_pre_rebuild(c, c->parity, c->stream);
+    if (st == DEM_OK) st = mixed_shadows(c, c->parity, c->stream);
+    if (st != DEM_OK) return st;
+  }
+  e = cudaStreamSynchronize(c->stream);
   return cuda_check(e, "dem_set_state");
 }
 
@@ -587,24 +597,20 @@ extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
   dem_status st = DEM_OK;
   int left = nsteps;
   if (c->opt.use_graph) {
-    /* graph replays start at shadow parity 0 */
-    if (c->parity != 0 && left > 0) {
-      st = host_step(c);
-      if (st != DEM_OK) return st;
-      left--;
-    }
-    if (left >= kGraphSteps) {
-      if (!c->graph_exec) {
-        st = build_graph(c, kGraphSteps);
+    const int G = graph_len(c);
+    const bool mixed = c->opt.precision == DEM_PREC_MIXED;
+    while (left >= G) {
+      const int p = mixed ? c->parity : 0;
+      if (!c->graph_exec[p]) {
+        st = build_graph(c, G, p);
         if (st != DEM_OK) return st;
       }
-      while (left >= kGraphSteps) {
-        cudaError_t e = cudaGraphLaunch(c->graph_exec, c->stream);
-        if (e != cudaSuccess) return cuda_check(e, "cudaGraphLaunch");
-        left -= kGraphSteps;
-        c->iter += kGraphSteps;
-        c->ctime += kGraphSteps * c->s.sim.dt;
-      }
+      cudaError_t e = cudaGraphLaunch(c->graph_exec[p], c->stream);
+      if (e != cudaSuccess) return cuda_check(e, "cudaGraphLaunch");
+      left -= G;
+      c->iter += G;
+      c->ctime += G * c->s.sim.dt;
+      if (mixed && (G & 1)) c->parity ^= 1;
     }
   }
   while (left > 0) {
@@ -613,6 +619,71 @@ extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
     left--;
   }
   return DEM_OK;
+}
+
+namespace dem {
+namespace {
+/* reads a buffer with 16-byte loads; the result is stored only under a
+ * condition the data cannot meet, so the loads are kept */
+__global__ void k_l2_read(const uint4* __restrict__ p, size_t n16, unsigned* __restrict__ sink) {
+  unsigned acc = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x) {
+    const uint4 v = p[i];
+    acc ^= v.x ^ v.y ^ v.z ^ v.w;
+  }
+  if (acc == 0x9E3779B9u && sink) *sink = acc;
+}
+}  // namespace
+}  // namespace dem
+
+extern "C" dem_status dem_l2_flush(void* stream, void* buf, size_t bytes) {
+  if (!buf || bytes < 64) return fail(DEM_ERR_ARG, "dem_l2_flush: bad buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t half = (bytes / 2) & ~(size_t)15;
+  cudaError_t e = cudaMemsetAsync(buf, 0x5a, half, s);
+  if (e != cudaSuccess) return cuda_check(e, "dem_l2_flush memset");
+  dem::k_l2_read<<<152 * 8, 256, 0, s>>>((const uint4*)((char*)buf + half), half / 16, (unsigned*)buf);
+  return cuda_check(cudaGetLastError(), "dem_l2_flush read");
+}
+
+extern "C" dem_status dem_profile_step(dem_ctx* c, int reps, void* flush_buf, size_t flush_bytes,
+                                       double* ms_avg) {
+  if (!c || reps <= 0 || !ms_avg) return fail(DEM_ERR_ARG, "dem_profile_step: bad argument");
+  cudaEvent_t e0, e1;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) return cuda_check(e, "dem_profile_step events");
+  double total = 0.0;
+  dem_status st = DEM_OK;
+  for (int r = 0; r < reps && st == DEM_OK; r++) {
+    if (flush_buf && flush_bytes) {
+      st = dem_l2_flush(c->stream, flush_buf, flush_bytes);
+      if (st != DEM_OK) break;
+    }
+    e = cudaEventRecord(e0, c->stream);
+    if (e != cudaSuccess) {
+      st = cuda_check(e, "dem_profile_step");
+      break;
+    }
+    st = enqueue_step(c, c->stream, c->parity);
+    if (st != DEM_OK) break;
+    e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) {
+      st = cuda_check(e, "dem_profile_step timing");
+      break;
+    }
+    total += ms;
+    if (c->opt.precision == DEM_PREC_MIXED) c->parity ^= 1;
+    c->iter++;
+    c->ctime += c->s.sim.dt;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st == DEM_OK) *ms_avg = total / reps;
+  return st;
 }
 
 extern "C" dem_status dem_sync(dem_ctx* c) {
@@ -709,6 +780,46 @@ extern "C" dem_status dem_get_history(dem_ctx* c, double* rec, int* brg, int max
       if (brg) brg[(size_t)i * max_per + a] = bf[(size_t)sl];
     }
   }
+  return DEM_OK;
+}
+
+extern "C" dem_status dem_get_aux(dem_ctx* c, double* pmove, int* lqd, int* nwall, int* wlist, double* wrec,
+                                  int* flag) {
+  if (!c) return fail(DEM_ERR_ARG, "dem_get_aux: null context");
+  const size_t N = (size_t)c->n;
+  if (c->opt.precision == DEM_PREC_MIXED) {
+    dem_status st = mixed_force_to_master(c, c->stream);
+    if (st != DEM_OK) return st;
+  }
+  std::vector<double> pm(N);
+  std::vector<int> lq(N), nw(N), wl(3 * N), id(N);
+  std::vector<ContactRec> wr(3 * N);
+  int fl = 0;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(pm.data(), c->b.pmove, sizeof(double) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(lq.data(), c->b.lqd, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(nw.data(), c->b.nwall, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(wl.data(), c->b.wlist, sizeof(int) * 3 * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(wr.data(), c->b.wrec, sizeof(ContactRec) * 3 * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(id.data(), c->b.id, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&fl, c->b.flag, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_check(e, "dem_get_aux");
+  for (size_t q = 0; q < N; q++) {
+    const int i = id[q];
+    if (pmove) pmove[i] = pm[q];
+    if (lqd) lqd[i] = lq[q];
+    if (nwall) nwall[i] = nw[q];
+    for (int a = 0; a < 3; a++) {
+      if (wlist) wlist[3 * (size_t)i + a] = wl[3 * q + a];
+      if (wrec) {
+        const ContactRec& x = wr[(size_t)a * N + q];
+        double* o = wrec + ((size_t)i * 3 + a) * 8;
+        o[0] = x.dx; o[1] = x.dy; o[2] = x.dz; o[3] = x.nDsp; o[4] = x.nDsp_mx; o[5] = x.plstRad;
+        o[6] = x.plstDfm; o[7] = (double)(int)(x.stage & 0xffffffff);
+      }
+    }
+  }
+  if (flag) *flag = fl;
   return DEM_OK;
 }
 

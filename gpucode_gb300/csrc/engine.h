@@ -77,9 +77,8 @@ struct dem_ctx {
   long long rebuilds_host;
   double ctime;
   dem::MixedState* mx;
-  /* CUDA graphs of a fixed number of steps (even), one per count */
-  cudaGraphExec_t graph_exec;
-  int graph_steps;
+  /* CUDA graphs of opt.graph_steps steps, one per starting shadow parity */
+  cudaGraphExec_t graph_exec[2];
   int parity; /* mixed: which shadow buffer the next step reads */
 };
 

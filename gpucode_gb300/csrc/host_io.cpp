@@ -648,13 +648,13 @@ extern "C" dem_status dem_pack_deposit(int n, const double* dia, double cx, doub
   double dmax = 0.0;
   for (int i = 0; i < n; i++) dmax = dia[i] > dmax ? dia[i] : dmax;
   if (!(dmax > 0.0) || 2.0 * R <= dmax) return dem::fail(DEM_ERR_ARG, "dem_pack_deposit: particles do not fit");
-  /* 2-D buckets over the disc; each keeps the spheres near its top surface:
-   * a falling sphere can only land on one whose top is within reach */
+  /* 2-D buckets over the disc; each keeps its spheres sorted by the height of
+   * their tops, so a falling sphere scans a bucket from the top down and stops
+   * as soon as no lower sphere could be reached (exact, no pruning) */
   const double cell = dmax + gap;
   const int g = (int)std::ceil(2.0 * R / cell) + 1;
   const double x0 = cx - R, y0 = cy - R;
   std::vector<std::vector<int>> bucket((size_t)g * g);
-  std::vector<double> btop((size_t)g * g, z0);
   uint64_t st = seed ? seed : 0x2545F4914F6CDD1Dull;
   auto uni = [&]() {
     uint64_t z = (st += 0x9E3779B97F4A7C15ull);
@@ -663,13 +663,13 @@ extern "C" dem_status dem_pack_deposit(int n, const double* dia, double cx, doub
     z ^= z >> 31;
     return (double)(z >> 11) * (1.0 / 9007199254740992.0);
   };
+  auto top_of = [&](int j) { return pos_out[j].z + 0.5 * dia[j]; };
   for (int i = 0; i < n; i++) {
     const double ri = 0.5 * dia[i];
     const double rr = R - ri - gap;
     if (rr <= 0.0) return dem::fail(DEM_ERR_ARG, "dem_pack_deposit: particle wider than the cylinder");
     double best_z = 1e300, bx = cx, by = cy;
     for (int t = 0; t < tries; t++) {
-      /* uniform point in the disc of radius rr */
       const double th = 2.0 * kPi * uni();
       const double rad = rr * std::sqrt(uni());
       const double x = cx + rad * std::cos(th), y = cy + rad * std::sin(th);
@@ -679,7 +679,11 @@ extern "C" dem_status dem_pack_deposit(int n, const double* dia, double cx, doub
         for (int dx = -1; dx <= 1; dx++) {
           const int bxi = ix + dx, byi = iy + dy;
           if (bxi < 0 || byi < 0 || bxi >= g || byi >= g) continue;
-          for (int j : bucket[(size_t)byi * g + bxi]) {
+          const std::vector<int>& L = bucket[(size_t)byi * g + bxi];
+          for (size_t r = L.size(); r-- > 0;) {
+            const int j = L[r];
+            /* the highest landing height sphere j can give is its top + ri + gap */
+            if (top_of(j) + ri + gap <= z) break;
             const double reach = ri + 0.5 * dia[j] + gap;
             const double hx = x - pos_out[j].x, hy = y - pos_out[j].y;
             const double h2 = hx * hx + hy * hy;
@@ -698,18 +702,10 @@ extern "C" dem_status dem_pack_deposit(int n, const double* dia, double cx, doub
     pos_out[i].y = by;
     pos_out[i].z = best_z;
     const int ix = (int)((bx - x0) / cell), iy = (int)((by - y0) / cell);
-    const size_t b = (size_t)iy * g + ix;
-    std::vector<int>& L = bucket[b];
+    std::vector<int>& L = bucket[(size_t)iy * g + ix];
+    /* insert keeping tops ascending (new spheres land near the top) */
     L.push_back(i);
-    if (best_z + ri > btop[b]) btop[b] = best_z + ri;
-    /* drop spheres buried deeper than two diameters under the bucket top */
-    if (L.size() > 24) {
-      const double floor_z = btop[b] - 2.0 * (dmax + gap) - dmax;
-      size_t w = 0;
-      for (size_t r = 0; r < L.size(); r++)
-        if (pos_out[L[r]].z + 0.5 * dia[L[r]] >= floor_z) L[w++] = L[r];
-      L.resize(w);
-    }
+    for (size_t r = L.size() - 1; r > 0 && top_of(L[r - 1]) > top_of(L[r]); r--) std::swap(L[r - 1], L[r]);
   }
   return DEM_OK;
 }

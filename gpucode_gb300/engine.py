@@ -63,7 +63,7 @@ class Engine:
     """One simulation on one GPU (dem_ctx)."""
 
     def __init__(self, setup: Setup, precision: str = "mixed", reorder: bool = True, use_graph: bool = True,
-                 capillary: str = "formula"):
+                 capillary: str = "formula", graph_steps: int = 0):
         self.lib = _abi.load()
         self.setup = setup
         opt = DemOptions()
@@ -72,6 +72,7 @@ class Engine:
         opt.capillary = {"formula": _abi.CAP_FORMULA, "mlp": _abi.CAP_MLP}[capillary]
         opt.reorder = 1 if reorder else 0
         opt.use_graph = 1 if use_graph else 0
+        opt.graph_steps = int(graph_steps)
         self.opt = opt
         h = C.c_void_p()
         check(self.lib.dem_create(C.byref(setup.s), ptr(setup.rad), ptr(setup.plevel), ptr(setup.nidx),

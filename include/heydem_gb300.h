@@ -261,7 +261,7 @@ typedef struct dem_options {
   int block_size;         /* threads per block of the step kernel (0 = default) */
   int reorder;            /* 1: keep particles in cell order (default); 0: reference order */
   int use_graph;          /* 1: replay steps through a CUDA graph (default) */
-  int seed;               /* reserved */
+  int graph_steps;        /* time steps per graph launch (0 = 16) */
 } dem_options;
 
 typedef struct dem_ctx dem_ctx;
@@ -285,12 +285,29 @@ dem_status dem_destroy(dem_ctx* c);
 /* Host state in the reference's double3 layout and particle order (reduced
  * units).  vel/angvel may be NULL (zero).  Marks the lists for rebuild. */
 dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel);
+/* As dem_set_state, but with request_rebuild = 0 the current neighbour lists,
+ * contact history and path-length accumulators are kept: for callers that
+ * round-trip the state through host memory between steps (the lists stay
+ * valid as long as no particle moved by more than the skin allowance). */
+dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel,
+                            int request_rebuild);
 /* Any pointer may be NULL.  force/mom are the last step's totals. */
 dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,
                          double3* mom);
 /* Advance nsteps time steps.  Device-resident; no host synchronisation inside
  * unless the context was created without graphs. */
 dem_status dem_step(dem_ctx* c, int nsteps);
+/* Time the force+integration kernel(s) of one step alone: reps launches on the
+ * context's stream, each bracketed by CUDA events; before each, flush_bytes of
+ * flush_buf (device memory, may be NULL) are overwritten so the launch starts
+ * with a cold L2.  The launches advance the simulation like dem_step without
+ * rebuilds.  *ms_avg receives the mean launch time in milliseconds. */
+dem_status dem_profile_step(dem_ctx* c, int reps, void* flush_buf, size_t flush_bytes, double* ms_avg);
+/* Evict the L2 cache for timing: on `stream` (a cudaStream_t), overwrite the
+ * first half of the device buffer, then read the second half, so the cache ends
+ * up holding clean lines of unrelated data (no write-backs charged to the next
+ * kernel).  bytes should be at least twice the L2 size. */
+dem_status dem_l2_flush(void* stream, void* buf, size_t bytes);
 /* Wait for the context's stream and check the device error word. */
 dem_status dem_sync(dem_ctx* c);
 dem_status dem_get_stats(dem_ctx* c, dem_stats* st);
@@ -305,6 +322,12 @@ dem_status dem_get_neighbors(dem_ctx* c, int* counts, int* partners, int max_per
  * rec[np*max_per][8] = dispt.x dispt.y dispt.z nDsp nDsp_mx plstRad plstDfm
  * stage, plus bridge flags brg[np*max_per]. */
 dem_status dem_get_history(dem_ctx* c, double* rec, int* brg, int max_per);
+/* The rest of the per-particle state, in the caller's order: path length since
+ * the last rebuild pmove[np], last step's bridge count lqd[np], wall list
+ * nwall[np] / wlist[np][3] (0 top, 1 bottom, 2 lateral) with its records
+ * wrec[np][3][8] (as dem_get_history), and the pending rebuild flag.  Any
+ * pointer may be NULL. */
+dem_status dem_get_aux(dem_ctx* c, double* pmove, int* lqd, int* nwall, int* wlist, double* wrec, int* flag);
 /* Write / read the full engine state (binary, with the reference's
  * "SYSTEM Info" text header so LoadPara can parse it). */
 dem_status dem_save(dem_ctx* c, const char* path, int nBatch);

@@ -649,6 +649,12 @@ void orc_sim_set_mode(orc_sim* s, int ForceCap, int stage) { s->ForceCap = Force
 void orc_sim_set_kernels(orc_sim* s, const orc_kernels* t) { s->kern = *t; }
 void orc_sim_request_rebuild(orc_sim* s) { s->need_build = 1; }
 
+void orc_sim_set_counter(orc_sim* s, const char* name, long v) {
+  if (!strcmp(name, "iter")) s->iter = v;
+  else if (!strcmp(name, "flag")) s->flag = (int)v;
+  else if (!strcmp(name, "need_build")) s->need_build = (int)v;
+}
+
 long orc_sim_counter(orc_sim* s, const char* name) {
   if (!strcmp(name, "iter")) return s->iter;
   if (!strcmp(name, "rebuilds")) return s->rebuilds;

@@ -148,6 +148,9 @@ void orc_sim_set_mode(orc_sim* s, int ForceCap, int stage);
 int orc_sim_step(orc_sim* s);
 /* counters: iter, rebuilds, last rebuild flag count */
 long orc_sim_counter(orc_sim* s, const char* name);
+/* set iter / flag (the last integration's rebuild count) / need_build, so a
+ * simulation can be resumed from another implementation's state */
+void orc_sim_set_counter(orc_sim* s, const char* name, long v);
 /* request a rebuild at the start of the next step (feed / restart path) */
 void orc_sim_request_rebuild(orc_sim* s);
 

@@ -1,0 +1,124 @@
+"""The native engine (dem_* API) on the GPU against the oracle, in lockstep
+(tests/_lockstep.py): before every step the oracle resumes from the engine's
+exact state, both step, the outputs are compared.
+
+FP64 mode (the reference formulas): neighbour lists (partner ids in the
+reference's list order), wall lists, load stages and bridge flags bit-exact,
+with or without cell reordering; forces, state and history to 1e-12 relative
+(last-ulp pow/log/exp differences between CUDA and glibc).
+Mixed mode (FP32 pair forces, Kahan-summed; FP64 state and spring history):
+forces to 2e-5 of the step's force scale, positions to 1e-9, velocities 2e-6,
+spins 2e-5, history to 1e-5;
+stage / bridge labels may differ where FP32 and FP64 round a comparison
+differently (a contact at its turning point), budgeted at 1%.
+Graph replay must equal host-driven stepping bit for bit, and a resumed
+checkpoint must equal the continuous run bit for bit."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import _lockstep
+import _workloads
+from gpucode_gb300 import _abi
+from gpucode_gb300.engine import Engine
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = {"force": 1e-12, "pos": 1e-14, "vel": 1e-12, "hist": 1e-12}
+# spins: a small sphere's moment of inertia 0.1 (2r)^5 is ~1e-4 of the largest,
+# so FP32 moment rounding shows amplified in its spin increment
+MIXED_TOL = {"force": 2e-5, "pos": 1e-9, "vel": 2e-6, "angvel": 2e-5, "hist": 1e-5}
+
+
+@pytest.mark.parametrize("make", [_workloads.small_dry, _workloads.small_wet])
+@pytest.mark.parametrize("reorder", [False, True])
+def test_fp64_engine_lockstep(cuda, make, reorder):
+    w = make()
+    pos, vel, ang = _workloads.stirred(w)
+    eng = Engine(w.setup, precision="fp64", reorder=reorder, use_graph=False)
+    worst = _lockstep.run(eng, w, pos, vel, ang, steps=250, tol=FP64_TOL)
+    assert worst["rebuilds"] >= 2, worst
+    eng.close()
+
+
+@pytest.mark.parametrize("make", [_workloads.small_dry, _workloads.small_wet])
+def test_mixed_engine_lockstep(cuda, make):
+    w = make()
+    pos, vel, ang = _workloads.stirred(w)
+    eng = Engine(w.setup, precision="mixed")
+    worst = _lockstep.run(eng, w, pos, vel, ang, steps=250, tol=MIXED_TOL, mismatch_budget=0.01)
+    assert worst["rebuilds"] >= 2, worst
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_replay_equals_host_stepping(cuda, precision):
+    w = _workloads.small_wet()
+    pos, vel, ang = _workloads.stirred(w)
+    a = Engine(w.setup, precision=precision, use_graph=True)
+    b = Engine(w.setup, precision=precision, use_graph=False)
+    for e in (a, b):
+        e.set_state(pos, vel, ang)
+        e.step(96)
+        e.sync()
+    sa, sb = a.get_state(), b.get_state()
+    for k in ("pos", "vel", "angvel"):
+        assert np.array_equal(sa[k], sb[k]), k
+    assert a.stats()["rebuilds"] == b.stats()["rebuilds"] >= 1
+    mp = _lockstep.max_per(w)
+    ha, hb = a.history(mp), b.history(mp)
+    assert np.array_equal(ha[0], hb[0]) and np.array_equal(ha[1], hb[1])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_checkpoint_resume_is_bit_exact(cuda, tmp_path, precision):
+    w = _workloads.small_wet()
+    pos, vel, ang = _workloads.stirred(w)
+    a = Engine(w.setup, precision=precision)
+    a.set_state(pos, vel, ang)
+    a.step(64)
+    path = tmp_path / "heyi_dump.dat"
+    a.save(path, nbatch=3)
+    a.step(64)
+    b = Engine(w.setup, precision=precision)
+    b.load(path)
+    b.step(64)
+    sa, sb = a.get_state(), b.get_state()
+    for k in ("pos", "vel", "angvel"):
+        assert np.array_equal(sa[k], sb[k]), k
+    # the dump keeps the reference's text header (DumpLoad.cpp:14-17)
+    lib = _abi.load()
+    x, y, z = C.c_int(), C.c_int(), C.c_int()
+    lib.LoadPara(str(path).encode(), C.byref(x), C.byref(y), C.byref(z))
+    assert (x.value, y.value, z.value) == (w.setup.n, 3, w.setup.n)
+
+
+def test_slot_overflow_is_reported_not_written(cuda):
+    """A level whose slot capacity is too small: the build stops at capacity and
+    dem_sync reports DEM_ERR_OVERFLOW (the reference would write past the end)."""
+    w = _workloads.small_dry()
+    s = w.setup
+    s.s.level_nnebors[0] = 2
+    s.s.n_pp_slots = 2 * s.s.level_npars[0]
+    pos, vel, ang = _workloads.stirred(w)
+    e = Engine(s, precision="mixed")
+    e.set_state(pos, vel, ang)
+    e.step(1)
+    with pytest.raises(_abi.DemError) as ei:
+        e.sync()
+    assert ei.value.code == _abi.DEM_ERR_OVERFLOW
+    counts, _ = e.neighbors(2)
+    assert counts.max() <= 2
+
+
+def test_nonfinite_state_is_reported(cuda):
+    w = _workloads.small_dry()
+    pos, vel, ang = _workloads.stirred(w)
+    vel[5, 1] = np.nan
+    e = Engine(w.setup, precision="mixed")
+    e.set_state(pos, vel, ang)
+    e.step(2)
+    with pytest.raises(_abi.DemError) as ei:
+        e.sync()
+    assert ei.value.code == _abi.DEM_ERR_NONFINITE
