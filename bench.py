@@ -177,6 +177,8 @@ def main():
     ap.add_argument("--profile-reps", type=int, default=20)
     ap.add_argument("--settle", type=int, default=2000,
                     help="untimed steps before the warm-up: gravity loads the deposited bed's contacts")
+    ap.add_argument("--no-fp64-check", dest="fp64_check", action="store_false",
+                    help="skip the FP64 rerun that gives the packing-fraction and coordination errors")
     ap.add_argument("--host-steps", action="store_true",
                     help="launch every step's kernels directly instead of from CUDA graphs (for ncu, which "
                          "cannot profile kernels of graphs with conditional nodes)")
@@ -245,6 +247,8 @@ def main():
     eng.sync()
     s1 = eng.stats()
     ms = sum(a.elapsed_time(b) for a, b in evs)
+    steps_run = args.settle + args.warmup + args.steps
+    pos_mixed = eng.get_state()["pos"]
     if ws > 1:
         t = torch.tensor([ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -287,6 +291,26 @@ def main():
     e2e = ws * n * E / e2e_t
     eng.sync()
 
+    # accuracy: the same bed, the same number of steps, all-FP64 reference formulas
+    accuracy = None
+    if rank == 0 and args.fp64_check:
+        from gpucode_gb300.engine import packing_metrics
+
+        ref = Engine(w.setup, precision="fp64", use_graph=True)
+        ref.set_state(w.pos0_reduced)
+        t0 = time.perf_counter()
+        ref.step(steps_run)
+        ref.sync()
+        t_fp64 = time.perf_counter() - t0
+        pos_ref = ref.get_state()["pos"]
+        ref.close()
+        mm, mr = packing_metrics(w.setup, pos_mixed), packing_metrics(w.setup, pos_ref)
+        accuracy = {"steps_compared": steps_run, "phi_mixed": mm["phi"], "phi_fp64": mr["phi"],
+                    "phi_rel_err": abs(mm["phi"] - mr["phi"]) / mr["phi"], "z_mixed": mm["z"], "z_fp64": mr["z"],
+                    "z_rel_err": abs(mm["z"] - mr["z"]) / max(mr["z"], 1e-300), "n_probe": mr["n_probe"],
+                    "fp64_particle_steps_per_s": n * steps_run / t_fp64,
+                    "max_position_diff": float(np.abs(pos_mixed - pos_ref).max())}
+
     if rank == 0:
         threads = os.cpu_count() or 1
         if args.cpu_steps > 0:
@@ -294,8 +318,8 @@ def main():
         else:
             cpu_val, cpu_sample = None, "skipped (--cpu-steps 0)"
         launches_per_step = 2  # decide + fused step kernel
-        rebuild_launches = 15  # lqd copy, copy_old, zero, hash, 3 scan, scatter, order, permute, copy_back,
-        #                        neighbour, wall list, carry, shadows
+        rebuild_launches = 14  # bridge counts, copy_old, hash, 3 scan, scatter, order, permute, copy_back,
+        #                        shadows, neighbour, wall list, carry
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": args.warmup,
             "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -315,6 +339,7 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * 72, "d2h_bytes_per_step": n * 96},
             "gpu_launches": launches_per_step * steps + rebuild_launches * d["rebuilds"],
             "clocks": ck,
+            "accuracy_vs_fp64": accuracy,
         }
         print(json.dumps(line), flush=True)
     eng.close()

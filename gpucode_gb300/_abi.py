@@ -197,6 +197,8 @@ def _declare(lib: C.CDLL) -> None:
         "dem_save": (I, [P, C.c_char_p, I]),
         "dem_load": (I, [P, C.c_char_p]),
         "dem_set_feed_seed": (None, [C.c_ulonglong]),
+        "dem_packing_metrics": (I, [I, P, P, P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(I)]),
+        "dem_l2_flush": (I, [P, P, C.c_size_t]),
         "dem_compat_errors": (I, []),
     }
     for name, (res, args) in sig.items():

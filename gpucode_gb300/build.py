@@ -27,6 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("errors.cpp", []),
     ("host_io.cpp", []),
+    ("metrics.cpp", []),
     ("build.cu", ["-fmad=false"]),
     ("step64.cu", ["-fmad=false"]),
     ("compat.cu", []),

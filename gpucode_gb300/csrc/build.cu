@@ -175,17 +175,27 @@ __global__ void k_cell_order(const int* __restrict__ sorted_hash, int* __restric
 }
 
 /* NeighborFindG (kernel.cu:729-855).  sorted_src == NULL means the particle
- * arrays are themselves in sorted order. */
+ * arrays are themselves in sorted order.
+ *
+ * Optional prefilter (pre.hi != NULL, particle arrays in sorted order): pre.hi
+ * holds (x, y, z, r) as the high floats of (coordinate + offset) with every
+ * coordinate in one binade, so hi_i - hi_j is exact in FP32; the FP32 distance
+ * from those differences is within pre.tol of the exact one.  A candidate
+ * farther than pre.tol from the cut-off is decided in FP32; only the band
+ * around it takes the reference's FP64 test, so the list is bit-identical to
+ * the all-FP64 build while almost no FP64 square roots are taken. */
 __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* __restrict__ rad,
                                 const int* __restrict__ sorted_src, const int* __restrict__ cell_start,
                                 const int* __restrict__ cell_end, const int* __restrict__ plevel,
                                 const int* __restrict__ nebor_idx, LevelView lv, double3 origin,
                                 double search_gap, int* __restrict__ nebor,
-                                int* __restrict__ num_nebor, int n, int* __restrict__ err) {
+                                int* __restrict__ num_nebor, int n, int* __restrict__ err, Prefilter pre) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double3 o = pos[i];
   const double ri = rad[i];
+  const float4 hi_i = pre.hi ? pre.hi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float sg = (float)search_gap;
   const int L = plevel[i];
   const long long base = slot_base(L, lv.level_npars, lv.level_nnebors) + nebor_idx[i];
   const long long stride = lv.level_npars[L];
@@ -218,6 +228,22 @@ __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* _
         for (int q = first; q < last; q++) {
           const int j = sorted_src ? sorted_src[q] : q;
           if (j == i) continue;
+          if (pre.hi) {
+            const float4 hj = pre.hi[j];
+            const float dx = hi_i.x - hj.x, dy = hi_i.y - hj.y, dz = hi_i.z - hj.z;
+            const float dc = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float cut = (hj.w + hi_i.w) + sg;
+            if (dc > cut + pre.tol) continue; /* certainly outside */
+            if (dc < cut - pre.tol) {         /* certainly inside */
+              if (count >= cap) {
+                over = true;
+                continue;
+              }
+              nebor[base + (long long)count * stride] = j;
+              count++;
+              continue;
+            }
+          }
           const double3 d = sub3(o, pos[j]);
           if (len3(d) < rad[j] + ri + search_gap) {
             if (count >= cap) {
@@ -375,11 +401,11 @@ dem_status cell_sort(const double3* pos, const int* plevel, const int* order_key
 dem_status neighbor_find(const double3* pos, const double* rad, const int* sorted_src,
                          const int* cell_start, const int* cell_end, const int* plevel, const int* nebor_idx,
                          LevelView lv, const DevConsts& k, int* nebor, int* num_nebor, int n, int* err,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, Prefilter pre) {
   if (n <= 0) return DEM_OK;
   k_neighbor_find<<<grid_for(n, 128), 128, 0, stream>>>(pos, rad, sorted_src, cell_start, cell_end, plevel,
                                                        nebor_idx, lv, k.prm.Origin, k.prm.SearchGap, nebor,
-                                                       num_nebor, n, err);
+                                                       num_nebor, n, err, pre);
   return cuda_check(cudaGetLastError(), "neighbor_find launch");
 }
 

@@ -74,6 +74,19 @@ struct __align__(16) ContactRec {
 };
 static_assert(sizeof(ContactRec) == 64, "ContactRec must be 64 bytes");
 
+/* The same 64-byte slot as the mixed-precision path lays it out: the tangential
+ * spring and the maximum overlap stay FP64 (they accumulate / are maxima over
+ * the contact's life); an FP32 copy of the spring feeds the FP32 contact math;
+ * the fields re-derived every step (current overlap, plastic radius and
+ * offset) are FP32. */
+struct __align__(16) MixedRec {
+  double dx, dy, dz, nDsp_mx;
+  float fx, fy, fz, nDsp;
+  float plstRad, plstDfm;
+  int stage, pad;
+};
+static_assert(sizeof(MixedRec) == 64, "MixedRec must be 64 bytes");
+
 /* history in the engine's layout */
 struct HistAoS {
   ContactRec* rec;
@@ -97,13 +110,21 @@ dem_status cell_sort(const double3* pos, const int* plevel, const int* order_key
                      int* sorted_src, int* cell_start, int* cell_end, void* scratch, int* err,
                      cudaStream_t stream);
 
+/* FP32 prefilter of the neighbour test (see build.cu): the high floats of
+ * (position + offset, radius) and the bound of their distance error */
+struct Prefilter {
+  const float4* hi;
+  float tol;
+};
+
 /* NeighborFindG semantics (kernel.cu:729-855) on AoS positions; sorted_src
  * maps sorted position -> particle index; writes the level/slot-major list.
  * Slot overflow sets bit 1 of *err and stops appending. */
 dem_status neighbor_find(const double3* pos, const double* rad, const int* sorted_src,
                          const int* cell_start, const int* cell_end, const int* plevel,
                          const int* nebor_idx, LevelView lv, const DevConsts& k, int* nebor,
-                         int* num_nebor, int n, int* err, cudaStream_t stream);
+                         int* num_nebor, int n, int* err, cudaStream_t stream,
+                         Prefilter pre = Prefilter{nullptr, 0.f});
 
 /* CirWallListG (kernel.cu:1034-1073); wall list pitched rows */
 dem_status wall_list(const double3* pos, const double* rad, const CylinderBC* cyl, int* wlist,

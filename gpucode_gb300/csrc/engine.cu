@@ -270,8 +270,15 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
     cudaError_t e = cudaMemsetAsync(b.pmove, 0, sizeof(double) * (size_t)n, s);
     if (e != cudaSuccess) return cuda_check(e, "pmove reset");
   }
+  Prefilter pre{nullptr, 0.f};
+  if (c->opt.precision == DEM_PREC_MIXED) {
+    /* the permuted state's shadows: read by the next step and by the build's prefilter */
+    st = mixed_shadows(c, parity, s);
+    if (st != DEM_OK) return st;
+    pre = mixed_prefilter(c, parity);
+  }
   st = neighbor_find(b.pos, b.rad, reorder ? nullptr : b.sorted_src, b.cell_start, b.cell_end, b.plevel, b.nidx,
-                     c->lv, c->k, b.nebor, b.num_nebor, n, b.err, s);
+                     c->lv, c->k, b.nebor, b.num_nebor, n, b.err, s, pre);
   if (st != DEM_OK) return st;
   st = wall_list(b.pos, b.rad, b.cyl, b.wlist, 3 * sizeof(int), b.nwall, n, c->k, s);
   if (st != DEM_OK) return st;
@@ -279,10 +286,7 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
                                            b.num_nebor_old, b.nidx_old, b.rec_old, b.brg_old, b.rec, b.brg, b.wlist,
                                            b.nwall, b.wlist_old, b.nwall_old, b.wrec_old, b.wrec,
                                            reorder ? b.sorted_src : nullptr, reorder ? b.old_to_new : nullptr, n);
-  st = cuda_check(cudaGetLastError(), "rebuild launch");
-  if (st != DEM_OK) return st;
-  if (c->opt.precision == DEM_PREC_MIXED) return mixed_shadows(c, parity, s);
-  return DEM_OK;
+  return cuda_check(cudaGetLastError(), "rebuild launch");
 }
 
 /* One step's force + integration kernels (graph-capturable). */
@@ -719,6 +723,19 @@ extern "C" dem_status dem_get_stats(dem_ctx* c, dem_stats* st) {
   return DEM_OK;
 }
 
+/* one history slot as dispt.xyz, nDsp, nDsp_mx, plstRad, plstDfm, stage */
+static void decode_record(const ContactRec& x, bool mixed, double* o) {
+  if (mixed) {
+    MixedRec m;
+    std::memcpy(&m, &x, sizeof(m));
+    o[0] = m.dx; o[1] = m.dy; o[2] = m.dz; o[3] = m.nDsp; o[4] = m.nDsp_mx; o[5] = m.plstRad;
+    o[6] = m.plstDfm; o[7] = (double)m.stage;
+  } else {
+    o[0] = x.dx; o[1] = x.dy; o[2] = x.dz; o[3] = x.nDsp; o[4] = x.nDsp_mx; o[5] = x.plstRad;
+    o[6] = x.plstDfm; o[7] = (double)(int)(x.stage & 0xffffffff);
+  }
+}
+
 extern "C" dem_status dem_get_neighbors(dem_ctx* c, int* counts, int* partners, int max_per) {
   if (!c || !counts || !partners || max_per <= 0) return fail(DEM_ERR_ARG, "dem_get_neighbors: bad argument");
   const size_t N = (size_t)c->n, S = (size_t)c->slots;
@@ -774,9 +791,7 @@ extern "C" dem_status dem_get_history(dem_ctx* c, double* rec, int* brg, int max
     for (int a = 0; a < num[q]; a++) {
       const long long sl = base[L] + (long long)a * c->s.level_npars[L] + nidx[q];
       double* o = rec + ((size_t)i * max_per + a) * 8;
-      const ContactRec& x = r[(size_t)sl];
-      o[0] = x.dx; o[1] = x.dy; o[2] = x.dz; o[3] = x.nDsp; o[4] = x.nDsp_mx; o[5] = x.plstRad;
-      o[6] = x.plstDfm; o[7] = (double)(int)(x.stage & 0xffffffff);
+      decode_record(r[(size_t)sl], c->opt.precision == DEM_PREC_MIXED, o);
       if (brg) brg[(size_t)i * max_per + a] = bf[(size_t)sl];
     }
   }
@@ -812,10 +827,7 @@ extern "C" dem_status dem_get_aux(dem_ctx* c, double* pmove, int* lqd, int* nwal
     for (int a = 0; a < 3; a++) {
       if (wlist) wlist[3 * (size_t)i + a] = wl[3 * q + a];
       if (wrec) {
-        const ContactRec& x = wr[(size_t)a * N + q];
-        double* o = wrec + ((size_t)i * 3 + a) * 8;
-        o[0] = x.dx; o[1] = x.dy; o[2] = x.dz; o[3] = x.nDsp; o[4] = x.nDsp_mx; o[5] = x.plstRad;
-        o[6] = x.plstDfm; o[7] = (double)(int)(x.stage & 0xffffffff);
+        decode_record(wr[(size_t)a * N + q], c->opt.precision == DEM_PREC_MIXED, wrec + ((size_t)i * 3 + a) * 8);
       }
     }
   }

@@ -89,6 +89,8 @@ dem_status mixed_create(dem_ctx* c);
 void mixed_destroy(dem_ctx* c);
 /* regenerate shadow buffer `which` from the FP64 master state */
 dem_status mixed_shadows(dem_ctx* c, int which, cudaStream_t s);
+/* the neighbour build's FP32 prefilter over shadow buffer `which` */
+Prefilter mixed_prefilter(dem_ctx* c, int which);
 /* one fused step reading shadows `which`, writing shadows 1 - which */
 dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s);
 /* copy the last step's bridge counts from the shadow `which` to the master */

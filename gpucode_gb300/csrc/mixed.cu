@@ -45,6 +45,8 @@ struct MixedState {
   float4* force;
   double3 off;
   float coarse_tol;
+  int bin_exp;    /* FP64 biased exponent of the binade [2^k, 2^(k+1)) */
+  float lo_scale; /* 2^(k-52): the weight of the last significand bit */
 };
 
 namespace {
@@ -79,6 +81,8 @@ struct MixArgs {
   const CylinderBC* cyl;
   int n, force_cap;
   double3 off;
+  int bin_exp;
+  float lo_scale;
   double dt, move_limit; /* 0.3 * SearchGap */
   float dtf, coarse_tol, rfrc;
   float lqd_vol, lqd_layer, lqd_gapmn, lqd_st;
@@ -119,13 +123,37 @@ __device__ __forceinline__ float two_sum(float a, float b, float& err) {
   return s;
 }
 
+/* ---- FP32 <-> FP64 through the integer pipe ----
+ * On GB300 FP64 conversions issue on the scarce FP64 pipe; these move the bits
+ * with integer operations instead.  d2f truncates the mantissa (error below one
+ * FP32 ulp) and flushes results below the FP32 normal range to zero; f2d is
+ * exact for normal floats.  Infinities and NaNs stay non-finite. */
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  const int e = (int)((u >> 52) & 0x7ff);
+  const int fe = e - 1023 + 127;
+  if (fe <= 0) return __uint_as_float(sign);
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u | (e == 0x7ff && (u & 0xfffffffffffffull) ? 1u : 0u));
+  return __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((u >> 29) & 0x7fffffu));
+}
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)sign);
+  const unsigned long long de = (e == 255) ? 0x7ffull : (unsigned long long)(e - 127 + 1023);
+  return __longlong_as_double((long long)(sign | (de << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+
 /* the elasto-plastic normal law, damping, tangential spring and rolling
- * resistance of kernel.cu:89-228 / :236-359 in FP32, with the spring held in
- * FP64 and advanced by FP32 increments */
-__device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, float3 u, float3 cpv, ContactRec& r,
+ * resistance of kernel.cu:89-228 / :236-359 in FP32.  The spring is advanced
+ * as an FP64 update by a small FP32 increment (three FP64 adds per contact);
+ * the maximum overlap stays an FP64 field. */
+__device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, float3 u, float3 cpv, MixedRec& r,
                                       float iRad, float rfrc, float dt, float3& dF, float3& dM, float& dR) {
-  const float plstDfm0 = (float)r.plstDfm, nDsp0 = (float)r.nDsp, nDspMx0 = (float)r.nDsp_mx;
-  float plstRad = (float)r.plstRad, plstDfm = plstDfm0, nDspMx = nDspMx0;
+  const float plstDfm0 = r.plstDfm, nDsp0 = r.nDsp, nDspMx0 = d2f(r.nDsp_mx);
+  float plstRad = r.plstRad, plstDfm = plstDfm0;
   int st;
   if (nrm < plstDfm0) st = 1;
   else if (nrm >= plstDfm0 && nrm < nDsp0) st = 3;
@@ -146,7 +174,7 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
       const float t = cbrtf(fN / (k43 * sqrtf(ijRad)));
       plstDfm = nrm - t * t;
     }
-    nDspMx = nrm;
+    r.nDsp_mx = f2d(nrm);
   } else if (st != 1) {
     const float t = nrm - plstDfm0;
     fN = k43 * sqrtf(plstRad) * (t * sqrtf(t));
@@ -155,12 +183,11 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
   const float fD = c.damp_on ? -2.0f * c.dmp * c.emod * sq * vn : 0.f;
   const float3 vt = cpv - vn * u;
 
-  /* spring: d_new = rescale(project(d)) + v_t dt, as an FP64 update by a
-   * small FP32 increment.  With cq = u.d, the projection is d - u cq and its
-   * length^2 is |d|^2 - cq^2, so the rescale factor minus one is
-   * cq^2 / ((|d| + |p|) |p|). */
-  const double3 d64 = make_double3(r.dx, r.dy, r.dz);
-  const float3 d = f3((float)d64.x, (float)d64.y, (float)d64.z);
+  /* spring: d_new = rescale(project(d)) + v_t dt.  With cq = u.d the
+   * projection is d - u cq, of length^2 |d|^2 - cq^2, so the rescale factor
+   * minus one is cq^2 / ((|d| + |p|) |p|): every term of the increment is
+   * small, and its FP32 error is relative to the increment, not the spring. */
+  const float3 d = f3(r.fx, r.fy, r.fz);
   const float cq = dotf(u, d);
   const float3 corr = f3(-u.x * cq, -u.y * cq, -u.z * cq);
   const float ld = lenf(d);
@@ -172,8 +199,8 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
   } else {
     inc = corr + vt * dt;
   }
-  double3 n64 = make_double3(d64.x + (double)inc.x, d64.y + (double)inc.y, d64.z + (double)inc.z);
-  float3 dn = d + inc;
+  double nx = r.dx + f2d(inc.x), ny = r.dy + f2d(inc.y), nz = r.dz + f2d(inc.z);
+  float3 dn = f3(d2f(nx), d2f(ny), d2f(nz));
   const float dsmx = 3.0f * c.sfrc * fN / (16.0f * (1.0f - c.pois) * c.emod / (4.0f - 2.0f * c.pois) * sq);
   float ratio = 1.0f;
   float ldn = lenf(dn);
@@ -184,15 +211,19 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
     }
   } else {
     const float f = (ldn > c.dsmx_eps) ? dsmx / ldn : dsmx;
-    n64.x *= (double)f;
-    n64.y *= (double)f;
-    n64.z *= (double)f;
-    dn = dn * f;
+    const double fd = f2d(f);
+    nx *= fd;
+    ny *= fd;
+    nz *= fd;
+    dn = f3(d2f(nx), d2f(ny), d2f(nz));
     ldn = lenf(dn);
   }
-  r.dx = n64.x;
-  r.dy = n64.y;
-  r.dz = n64.z;
+  r.dx = nx;
+  r.dy = ny;
+  r.dz = nz;
+  r.fx = dn.x;
+  r.fy = dn.y;
+  r.fz = dn.z;
   float3 fT = f3(0.f, 0.f, 0.f);
   if (ldn < dsmx) {
     if (ldn > 1.0e-10f) fT = dn * (-c.sfrc * fN * ratio / ldn);
@@ -204,10 +235,9 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
   const float arm = iRad - nrm * 0.5f;
   dM = crossf(u * (-arm), fT);
   dR = 0.5f * (rfrc + rfrc) * fN * iRad;
-  r.nDsp = (double)nrm;
-  r.nDsp_mx = (double)nDspMx;
-  r.plstRad = (double)plstRad;
-  r.plstDfm = (double)plstDfm;
+  r.nDsp = nrm;
+  r.plstRad = plstRad;
+  r.plstDfm = plstDfm;
   r.stage = st;
 }
 
@@ -224,20 +254,38 @@ __device__ __forceinline__ float fcap32(float Splus, float ijVol, float effR, fl
   return 2.0f * kPiF * effR * st * expf(f1 - f2 * expf(f3 * ls + f4 * ls * ls));
 }
 
-__device__ __forceinline__ ContactRec load_rec(const ContactRec* p) {
-  const double2* q = reinterpret_cast<const double2*>(p);
-  const double2 a = q[0], b = q[1], c = q[2], d = q[3];
-  ContactRec r;
-  r.dx = a.x; r.dy = a.y; r.dz = b.x; r.nDsp = b.y; r.nDsp_mx = c.x; r.plstRad = c.y; r.plstDfm = d.x;
-  r.stage = __double_as_longlong(d.y);
+__device__ __forceinline__ MixedRec load_rec(const ContactRec* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  MixedRec r;
+  float4* o = reinterpret_cast<float4*>(&r);
+  o[0] = q[0];
+  o[1] = q[1];
+  o[2] = q[2];
+  o[3] = q[3];
   return r;
 }
-__device__ __forceinline__ void store_rec(ContactRec* p, const ContactRec& r) {
-  double2* q = reinterpret_cast<double2*>(p);
-  q[0] = make_double2(r.dx, r.dy);
-  q[1] = make_double2(r.dz, r.nDsp);
-  q[2] = make_double2(r.nDsp_mx, r.plstRad);
-  q[3] = make_double2(r.plstDfm, __longlong_as_double(r.stage));
+__device__ __forceinline__ void store_rec(ContactRec* p, const MixedRec& r) {
+  float4* q = reinterpret_cast<float4*>(p);
+  const float4* o = reinterpret_cast<const float4*>(&r);
+  q[0] = o[0];
+  q[1] = o[1];
+  q[2] = o[2];
+  q[3] = o[3];
+}
+
+/* hi/lo split of a coordinate already shifted into the binade [2^k, 2^(k+1)):
+ * hi keeps the top 24 significand bits (exponent fixed), lo the remaining 29
+ * bits as an exact integer times 2^(k-52), rounded to 24 bits.  Integer and
+ * conversion units only; a value outside the binade takes the FP64 route. */
+__device__ __forceinline__ void split_hi_lo(double xo, int dexp, float lo_scale, float& hi, float& lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(xo);
+  if ((int)((u >> 52) & 0x7ff) == dexp && !(u >> 63)) {
+    hi = __uint_as_float(((unsigned)(dexp - 1023 + 127) << 23) | (unsigned)((u >> 29) & 0x7fffffu));
+    lo = __uint2float_rn((unsigned)(u & 0x1fffffffull)) * lo_scale;
+  } else {
+    hi = (float)xo;
+    lo = (float)(xo - (double)hi);
+  }
 }
 
 __device__ __forceinline__ void warp_add(unsigned long long* ctr, unsigned v) {
@@ -312,7 +360,7 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
         const float3 jv = f3(vj4.x, vj4.y, vj4.z), jw = f3(wj4.x, wj4.y, wj4.z);
         const float3 cpv = (iv - jv) - crossf(iw * ri + jw * rj, u);
         const float ijRad = ri * rj / (ri + rj);
-        ContactRec rc = load_rec(a.rec + s);
+        MixedRec rc = load_rec(a.rec + s);
         float3 dF, dM;
         float dR;
         law32(a.pp, ijRad, -gap, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
@@ -376,7 +424,7 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
         const float3 u = f3((float)d.x * il, (float)d.y * il, (float)d.z * il);
         const float3 cpv = (iv - f3((float)jvel.x, (float)jvel.y, (float)jvel.z)) - crossf(iw * ri, u);
         ContactRec* rp = a.wrec + (long long)w * a.n + qq;
-        ContactRec rc = load_rec(rp);
+        MixedRec rc = load_rec(rp);
         float3 dF, dM;
         float dR;
         law32(a.pw, ri, -gapw, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
@@ -392,32 +440,39 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
   /* integrator (UpdateSystemG) in FP64 with FP32 increments */
   bool flagged = false;
   if (live) {
+    /* 13 FP64 operations per particle: v += dv (3), x += v dt (3), path
+     * length (1), spin (3), binade shift of the shadow (3); every conversion
+     * goes through the integer pipe */
     const float fx = F.x.s - F.x.c, fy = F.y.s - F.y.c, fz = F.z.s - F.z.c;
     const float inv_m = a.dtf / mass_f;
     double3 v = a.vel[q];
-    v.x += (double)(fx * inv_m);
-    v.y += (double)(fy * inv_m);
-    v.z += (double)(fz * inv_m);
+    v.x += f2d(fx * inv_m);
+    v.y += f2d(fy * inv_m);
+    v.z += f2d(fz * inv_m);
     p.x = fma(v.x, a.dt, p.x);
     p.y = fma(v.y, a.dt, p.y);
     p.z = fma(v.z, a.dt, p.z);
-    const float vxf = (float)v.x, vyf = (float)v.y, vzf = (float)v.z;
-    const double pm = a.pmove[q] + (double)(sqrtf(vxf * vxf + vyf * vyf + vzf * vzf) * a.dtf);
+    const float vxf = d2f(v.x), vyf = d2f(v.y), vzf = d2f(v.z);
+    const double pm = a.pmove[q] + f2d(sqrtf(vxf * vxf + vyf * vyf + vzf * vzf) * a.dtf);
     const float inert = 0.1f * mass_f * twor * twor;
     const float inv_i = a.dtf / inert;
     double3 w = a.angv[q];
-    w.x += (double)((M.x.s - M.x.c) * inv_i);
-    w.y += (double)((M.y.s - M.y.c) * inv_i);
-    w.z += (double)((M.z.s - M.z.c) * inv_i);
+    /* spin: w += M dt / I, then the rolling-resistance damping
+     * w *= 1 - min(1, Mr dt / I / |w|), folded into one increment */
+    const float dwx = (M.x.s - M.x.c) * inv_i, dwy = (M.y.s - M.y.c) * inv_i, dwz = (M.z.s - M.z.c) * inv_i;
     const float rm = (R.s - R.c) * inv_i;
-    const float wxf = (float)w.x, wyf = (float)w.y, wzf = (float)w.z;
-    const float wl = sqrtf(wxf * wxf + wyf * wyf + wzf * wzf);
+    const float wx1 = wi4.x + dwx, wy1 = wi4.y + dwy, wz1 = wi4.z + dwz;
+    const float wl = sqrtf(wx1 * wx1 + wy1 * wy1 + wz1 * wz1);
+    float ix = dwx, iy = dwy, iz = dwz;
     if (wl > 1.0e-7f) {
       const float f = fminf(1.0f, rm / wl);
-      w.x -= (double)(wxf * f);
-      w.y -= (double)(wyf * f);
-      w.z -= (double)(wzf * f);
+      ix -= wx1 * f;
+      iy -= wy1 * f;
+      iz -= wz1 * f;
     }
+    w.x += f2d(ix);
+    w.y += f2d(iy);
+    w.z += f2d(iz);
     a.vel[q] = v;
     a.pos[q] = p;
     a.angv[q] = w;
@@ -425,12 +480,16 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
     flagged = pm > a.move_limit;
     if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(a.err, 2);
     /* next step's shadows */
-    const double xo = p.x + a.off.x, yo = p.y + a.off.y, zo = p.z + a.off.z;
-    const float xh = (float)xo, yh = (float)yo, zh = (float)zo;
-    a.phi_out[q] = make_float4(xh, yh, zh, hi.w);
-    a.plo_out[q] = make_float4((float)(xo - (double)xh), (float)(yo - (double)yh), (float)(zo - (double)zh), lo.w);
-    a.v_out[q] = make_float4((float)v.x, (float)v.y, (float)v.z, __int_as_float(wet));
-    a.w_out[q] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
+    float4 ph, pl;
+    split_hi_lo(p.x + a.off.x, a.bin_exp, a.lo_scale, ph.x, pl.x);
+    split_hi_lo(p.y + a.off.y, a.bin_exp, a.lo_scale, ph.y, pl.y);
+    split_hi_lo(p.z + a.off.z, a.bin_exp, a.lo_scale, ph.z, pl.z);
+    ph.w = hi.w;
+    pl.w = lo.w;
+    a.phi_out[q] = ph;
+    a.plo_out[q] = pl;
+    a.v_out[q] = make_float4(vxf, vyf, vzf, __int_as_float(wet));
+    a.w_out[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
     a.force_out[q] = make_float4(fx, fy, fz, 0.f);
   }
   const unsigned fm = __ballot_sync(0xffffffffu, flagged);
@@ -445,21 +504,23 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
 
 __global__ void k_shadows(int n, const double3* __restrict__ pos, const double3* __restrict__ vel,
                           const double3* __restrict__ angv, const double* __restrict__ rad, const int* __restrict__ lqd,
-                          double3 off, float4* __restrict__ phi, float4* __restrict__ plo, float4* __restrict__ v4,
-                          float4* __restrict__ w4) {
+                          double3 off, int bin_exp, float lo_scale, float4* __restrict__ phi, float4* __restrict__ plo,
+                          float4* __restrict__ v4, float4* __restrict__ w4) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   const double3 p = pos[q];
-  const double xo = p.x + off.x, yo = p.y + off.y, zo = p.z + off.z;
-  const float xh = (float)xo, yh = (float)yo, zh = (float)zo;
+  float4 ph, pl;
+  split_hi_lo(p.x + off.x, bin_exp, lo_scale, ph.x, pl.x);
+  split_hi_lo(p.y + off.y, bin_exp, lo_scale, ph.y, pl.y);
+  split_hi_lo(p.z + off.z, bin_exp, lo_scale, ph.z, pl.z);
   const double r = rad[q];
-  const float rh = (float)r;
-  phi[q] = make_float4(xh, yh, zh, rh);
-  plo[q] = make_float4((float)(xo - (double)xh), (float)(yo - (double)yh), (float)(zo - (double)zh),
-                       (float)(r - (double)rh));
+  ph.w = (float)r;
+  pl.w = (float)(r - (double)ph.w);
+  phi[q] = ph;
+  plo[q] = pl;
   const double3 v = vel[q], w = angv[q];
-  v4[q] = make_float4((float)v.x, (float)v.y, (float)v.z, __int_as_float(lqd[q]));
-  w4[q] = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
+  v4[q] = make_float4(d2f(v.x), d2f(v.y), d2f(v.z), __int_as_float(lqd[q]));
+  w4[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
 }
 
 __global__ void k_force_out(int n, const float4* __restrict__ f, double3* __restrict__ force, double3* __restrict__ mom) {
@@ -519,6 +580,8 @@ dem_status mixed_create(dem_ctx* c) {
   /* the hi-part-only overlap estimate is off by at most |lo_i - lo_j| per
    * axis, below two ulps of the binade: four ulps is a safe candidate margin */
   m->coarse_tol = (float)(4.0 * std::ldexp(1.0, k2 - 23));
+  m->bin_exp = 1023 + k2;
+  m->lo_scale = (float)std::ldexp(1.0, k2 - 52);
   return DEM_OK;
 }
 
@@ -530,9 +593,17 @@ void mixed_destroy(dem_ctx* c) {
 dem_status mixed_shadows(dem_ctx* c, int which, cudaStream_t s) {
   MixedState* m = c->mx;
   EngineBufs& b = c->b;
-  k_shadows<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, b.pos, b.vel, b.angv, b.rad, b.lqd, m->off, m->phi[which],
+  k_shadows<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, b.pos, b.vel, b.angv, b.rad, b.lqd, m->off, m->bin_exp,
+                                                 m->lo_scale, m->phi[which],
                                                  m->plo[which], m->vel[which], m->angv[which]);
   return cuda_check(cudaGetLastError(), "mixed_shadows launch");
+}
+
+Prefilter mixed_prefilter(dem_ctx* c, int which) {
+  /* |(hi_i - hi_j) - (x_i - x_j)| <= one binade ulp per axis (the lo parts are
+   * below half an ulp each): sqrt(3) ulps, plus FP32 rounding of the distance
+   * and of the cut-off (~3e-7 relative, distances < 4 reduced units) */
+  return Prefilter{c->mx->phi[which], 0.5f * c->mx->coarse_tol + 2.0e-6f};
 }
 
 dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
@@ -550,6 +621,8 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   a.n = c->n;
   a.force_cap = c->s.force_cap;
   a.off = m->off;
+  a.bin_exp = m->bin_exp;
+  a.lo_scale = m->lo_scale;
   a.dt = c->s.prm.dt;
   a.dtf = (float)c->s.prm.dt;
   a.move_limit = 0.3 * c->s.prm.SearchGap;

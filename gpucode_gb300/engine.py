@@ -59,6 +59,18 @@ class Setup:
         return np.asarray(x_m, np.float64) / self.s.unit.rlunit
 
 
+def packing_metrics(setup: Setup, pos: np.ndarray) -> dict:
+    """Packing fraction and mean coordination number of a bed (dem_packing_metrics)."""
+    lib = _abi.load()
+    p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+    phi, z = C.c_double(), C.c_double()
+    npb = C.c_int()
+    check(lib.dem_packing_metrics(len(p), ptr(p), ptr(np.ascontiguousarray(setup.rad, np.float64)),
+                                  C.byref(setup.s.cyl), C.byref(phi), C.byref(z), C.byref(npb)),
+          "dem_packing_metrics")
+    return {"phi": phi.value, "z": z.value, "n_probe": npb.value}
+
+
 class Engine:
     """One simulation on one GPU (dem_ctx)."""
 

@@ -348,6 +348,13 @@ int dem_compat_errors(void);
  * dia[n] and pos_out[n] in the same (any) length unit. */
 dem_status dem_pack_deposit(int n, const double* dia, double cx, double cy, double R, double z0,
                             double gap, int tries, unsigned long long seed, double3* pos_out);
+/* Packing fraction and mean coordination number of a bed (host, any units):
+ * probe cylinder coaxial with the container, radius R - 3 d_max, from
+ * Bw + 3 d_max to 3 d_max below the free surface (98th percentile of sphere
+ * tops); spheres clipped exactly by the probe; Z = mean number of overlapping
+ * p-p contacts of the spheres centred in the probe. */
+dem_status dem_packing_metrics(int n, const double3* pos, const double* rad, const CylinderBC* cyl, double* phi,
+                               double* z_mean, int* n_probe);
 /* Struct sizes and offsets of this header, for binding checks. */
 int dem_abi_layout(long long* out, int cap);
 
