@@ -358,3 +358,76 @@ void PPCntHstryCopy(PPCONTACT_HISTORY old_h, PPCONTACT_HISTORY cur_h, int nPPCnt
 }
 
 }  // extern "C"
+
+/* ---------------- BldNeborList without device allocation ----------------
+ *
+ * Some callers may not allocate device memory while they step: a driver that
+ * reserves the card's memory once, up front, for a fixed plan of particle
+ * buffers, and loops that cannot take the device-wide synchronisation that
+ * cudaFree implies (BldNeborList above frees and re-allocates its scratch cache
+ * when the particle count grows; the reference's thrust sort allocates on every
+ * call).  BldNeborListNoAlloc gives them the same neighbour build with the
+ * cell sort's scratch in a fixed array of device memory that the library image
+ * carries, so the call itself never allocates. */
+
+namespace {
+
+/* 16 MiB: the sort's keys and ranks (2 ints per particle), one int per scan
+ * tile of 2048 cells and 64 spare ints -- about 2 million particles.  Nothing
+ * in it has to start at zero: within one call every word is written before it
+ * is read. */
+constexpr size_t kStaticSortScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_static_sort_scratch[kStaticSortScratchBytes];
+
+/* its address on each device, looked up once per device */
+constexpr int kMaxStaticDevices = 64;
+std::mutex g_static_mu;
+void* g_static_scratch_at[kMaxStaticDevices] = {};
+
+dem_status static_scratch(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return dem::cuda_check(e, "BldNeborListNoAlloc: cudaGetDevice");
+  if (dev < 0 || dev >= kMaxStaticDevices)
+    return dem::fail(DEM_ERR_ARG, "BldNeborListNoAlloc: device index " + std::to_string(dev) +
+                                      " is beyond the " + std::to_string(kMaxStaticDevices) + " it tracks");
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_scratch_at[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_sort_scratch);
+    if (e != cudaSuccess) return dem::cuda_check(e, "BldNeborListNoAlloc: cudaGetSymbolAddress");
+    if (!p) return dem::fail(DEM_ERR_CUDA, "BldNeborListNoAlloc: the static scratch has no device address");
+    g_static_scratch_at[dev] = p;
+  }
+  *out = g_static_scratch_at[dev];
+  return DEM_OK;
+}
+
+}  // namespace
+
+extern "C" int BldNeborListNoAlloc(int* hash, int* index, int* cellStart, int* cellEnd, int* d_pLevel,
+                                   SEARCHCELL d_cell, int* d_Ncell_Idx, double* d_Level_size,
+                                   int* d_level_nPars, int* d_level_nNebors, int nLevels, double3* pos,
+                                   int Sys_nCells, int* d_Nebor1, int* d_Nebor_Idx, int* d_Num_Nebor,
+                                   int TotalParticle, double* rad, int* d_err) {
+  if (TotalParticle < 0 || Sys_nCells <= 0 || nLevels <= 0)
+    return dem::fail(DEM_ERR_ARG, "BldNeborListNoAlloc: bad sizes (TotalParticle " + std::to_string(TotalParticle) +
+                                      ", Sys_nCells " + std::to_string(Sys_nCells) + ", nLevels " +
+                                      std::to_string(nLevels) + ")");
+  if (!d_err) return dem::fail(DEM_ERR_ARG, "BldNeborListNoAlloc: d_err is NULL (pass a zeroed device int)");
+  const size_t need = dem::sort_scratch_bytes(TotalParticle, Sys_nCells);
+  if (need > kStaticSortScratchBytes)
+    return dem::fail(DEM_ERR_ARG, "BldNeborListNoAlloc: " + std::to_string(TotalParticle) + " particles and " +
+                                      std::to_string(Sys_nCells) + " cells need " + std::to_string(need) +
+                                      " bytes of sort scratch; the static scratch holds " +
+                                      std::to_string(kStaticSortScratchBytes) + " (use BldNeborList)");
+  void* scratch = nullptr;
+  dem_status st = static_scratch(&scratch);
+  if (st != DEM_OK) return st;
+  dem::LevelView lv = view(d_cell, d_Ncell_Idx, d_Level_size, d_level_nPars, d_level_nNebors, nLevels);
+  st = dem::cell_sort(pos, d_pLevel, nullptr, TotalParticle, lv, g_consts, Sys_nCells, hash, index, cellStart,
+                      cellEnd, scratch, d_err, 0);
+  if (st != DEM_OK) return st;
+  return dem::neighbor_find(pos, rad, index, cellStart, cellEnd, d_pLevel, d_Nebor_Idx, lv, g_consts, d_Nebor1,
+                            d_Num_Nebor, TotalParticle, d_err, 0);
+}

@@ -341,6 +341,27 @@ void dem_set_feed_seed(unsigned long long seed);
  * reference would write past it, kernel.cu:833-836), bit 4 = a particle hashed
  * outside the cell grid. */
 int dem_compat_errors(void);
+/* BldNeborList (above) without any device allocation.  No counterpart in the
+ * reference: its BldNeborList sorts with thrust, which allocates temporary
+ * storage on every call, and this library's BldNeborList keeps a scratch cache
+ * that it frees and re-allocates when the particle count grows.
+ *
+ * Same arguments and outputs as BldNeborList, plus d_err: one device int the
+ * caller owns, which must be zero before the first call; the kernels OR bit 1
+ * (a neighbour list stopped at its level's slot capacity) and bit 4 (a
+ * particle hashed outside the cell grid) into it and never clear it.  The
+ * cell sort's scratch is a fixed 16 MiB array of device memory inside the
+ * library: 4 * (2 * TotalParticle + ceil(Sys_nCells / 2048) + 64) bytes must
+ * fit, i.e. up to about 2,000,000 particles; larger sizes return DEM_ERR_ARG
+ * with a message and launch nothing.  The first call on each device looks the
+ * array's address up (make it before any stream capture).  Calls share that
+ * one array: two calls whose kernels run at the same time on one device race.
+ * Returns DEM_OK or a negative dem_status (see dem_last_error). */
+int BldNeborListNoAlloc(int* d_GridParticleHash, int* d_GridParticleIndex, int* d_CellStart,
+                        int* d_CellEnd, int* d_pLevel, SEARCHCELL d_cell, int* d_Ncell_Idx,
+                        double* d_Level_size, int* d_level_nPars, int* d_level_nNebors, int nLevels,
+                        double3* dPos, int Sys_nCells, int* d_Nebor1, int* d_Nebor_Idx,
+                        int* d_Num_Nebor, int TotalParticle, double* dRad, int* d_err);
 /* Seeded sequential deposition into a cylinder (test / benchmark inputs):
  * particles in the given order are dropped at the lowest of `tries` random
  * (x, y) candidates inside radius R - r of the axis (cx, cy) onto the floor z0
