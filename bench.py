@@ -179,6 +179,8 @@ def main():
                     help="untimed steps before the warm-up: gravity loads the deposited bed's contacts")
     ap.add_argument("--no-fp64-check", dest="fp64_check", action="store_false",
                     help="skip the FP64 rerun that gives the packing-fraction and coordination errors")
+    ap.add_argument("--ref-gpu-steps", type=int, default=40,
+                    help="timed steps of the reference's own kernels on this GPU (0: skip)")
     ap.add_argument("--host-steps", action="store_true",
                     help="launch every step's kernels directly instead of from CUDA graphs (for ncu, which "
                          "cannot profile kernels of graphs with conditional nodes)")
@@ -311,6 +313,32 @@ def main():
                     "fp64_particle_steps_per_s": n * steps_run / t_fp64,
                     "max_position_diff": float(np.abs(pos_mixed - pos_ref).max())}
 
+    # the reference's own kernels (kernel.cu built for sm_103a) on this GPU, same bed
+    ref_gpu = None
+    if rank == 0 and args.ref_gpu_steps > 0:
+        from baseline import refgpu
+
+        ok, why = refgpu.available()
+        if not ok:
+            ref_gpu = {"unavailable": why}
+        else:
+            stt = eng.get_state()
+            try:
+                r, _ = refgpu.run(w.setup, stt["pos"], stt["vel"], stt["angvel"], 5, args.ref_gpu_steps,
+                                  flush.data_ptr(), flush.numel())
+                rv = n / (r["step_ms"] * 1e-3)
+                ref_gpu = {"value": rv, "unit": UNIT, "ms_per_step": r["step_ms"],
+                           "kernel_ms": {"PPForceCalcG": r["force_ms"], "CirPWInterG": r["wall_ms"],
+                                         "UpdateSystemG": r["update_ms"]},
+                           "rebuilds": r["rebuilds"], "slot_overflow": bool(r["overflow"]),
+                           "speedup": value / rv,
+                           "kernel_speedup": (r["force_ms"] + r["wall_ms"] + r["update_ms"]) / ms_k.value,
+                           "sample": f"{args.ref_gpu_steps} steps after 5 warm-up from this bed's final state, "
+                                     "histories empty, L2 evicted before each step, main.cpp step order "
+                                     "(per-step flag read, VarInit memsets)"}
+            except RuntimeError as e:
+                ref_gpu = {"unavailable": str(e)}
+
     if rank == 0:
         threads = os.cpu_count() or 1
         if args.cpu_steps > 0:
@@ -340,6 +368,7 @@ def main():
             "gpu_launches": launches_per_step * steps + rebuild_launches * d["rebuilds"],
             "clocks": ck,
             "accuracy_vs_fp64": accuracy,
+            "reference_kernels_gpu": ref_gpu,
         }
         print(json.dumps(line), flush=True)
     eng.close()

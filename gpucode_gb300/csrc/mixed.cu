@@ -59,6 +59,7 @@ constexpr float kPiF = 3.1415926f;
 struct Law32 {
   float emod, pois, sfrc, ydsp, yforce, ystiff;
   float rot_eps, dsmx_eps;
+  float kt;      /* 16 (1 - pois) emod / (4 - 2 pois): slip-distance denominator */
   float dmp;     /* sqrt(dmpn product) */
   int hertz_le;  /* p-p: <=, wall: < */
   int damp_on;
@@ -194,23 +195,24 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
   const float lp = lenf(d + corr);
   float3 inc;
   if (lp > c.rot_eps) {
-    const float sm1 = (cq * cq) / ((ld + lp) * lp);
+    const float sm1 = __fdividef(cq * cq, (ld + lp) * lp);
     inc = corr * (1.0f + sm1) + d * sm1 + vt * dt;
   } else {
     inc = corr + vt * dt;
   }
   double nx = r.dx + f2d(inc.x), ny = r.dy + f2d(inc.y), nz = r.dz + f2d(inc.z);
   float3 dn = f3(d2f(nx), d2f(ny), d2f(nz));
-  const float dsmx = 3.0f * c.sfrc * fN / (16.0f * (1.0f - c.pois) * c.emod / (4.0f - 2.0f * c.pois) * sq);
+  const float dsmx = __fdividef(3.0f * c.sfrc * fN, c.kt * sq);
   float ratio = 1.0f;
   float ldn = lenf(dn);
   if (ldn < dsmx) {
     if (dsmx > c.dsmx_eps) {
-      const float t = 1.0f - ldn / dsmx;
+      /* the approximate quotient may round above 1 just below the slip limit */
+      const float t = fmaxf(0.0f, 1.0f - __fdividef(ldn, dsmx));
       ratio = 1.0f - t * sqrtf(t);
     }
   } else {
-    const float f = (ldn > c.dsmx_eps) ? dsmx / ldn : dsmx;
+    const float f = (ldn > c.dsmx_eps) ? __fdividef(dsmx, ldn) : dsmx;
     const double fd = f2d(f);
     nx *= fd;
     ny *= fd;
@@ -226,10 +228,10 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
   r.fz = dn.z;
   float3 fT = f3(0.f, 0.f, 0.f);
   if (ldn < dsmx) {
-    if (ldn > 1.0e-10f) fT = dn * (-c.sfrc * fN * ratio / ldn);
+    if (ldn > 1.0e-10f) fT = dn * __fdividef(-c.sfrc * fN * ratio, ldn);
   } else {
     const float lvt = lenf(vt);
-    if (lvt > 1.0e-10f) fT = vt * (-c.sfrc * fN * ratio / lvt);
+    if (lvt > 1.0e-10f) fT = vt * __fdividef(-c.sfrc * fN * ratio, lvt);
   }
   dF = (fN + fD) * u + fT;
   const float arm = iRad - nrm * 0.5f;
@@ -241,17 +243,19 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
   r.stage = st;
 }
 
-/* kernel.cu:65-81 in FP32 */
+/* kernel.cu:65-81 in FP32.  The hardware approximations of log and exp are
+ * used: their errors (a few ulp, relative) stay far below the FP32 force
+ * tolerance, and the regression they feed is itself a fit. */
 __device__ __forceinline__ float fcap32(float Splus, float ijVol, float effR, float gapmn, float st) {
   Splus = fmaxf(gapmn, Splus);
-  Splus = Splus / sqrtf(ijVol);
-  const float L = logf(ijVol), L2 = L * L, L3 = L2 * L;
+  Splus = Splus * rsqrtf(ijVol);
+  const float L = __logf(ijVol), L2 = L * L, L3 = L2 * L;
   const float f1 = -0.44507f - 0.1119f * L - 0.012101f * L2 - 0.0005f * L3;
   const float f2 = 1.9222f - 0.0668f * L - 0.0013375f * L2;
   const float f3 = 1.268f + 0.198f * L + 0.02232f * L2 + 0.0008585f * L3;
   const float f4 = -0.010703f + 0.03345f * L + 0.0018574f * L2;
-  const float ls = logf(Splus);
-  return 2.0f * kPiF * effR * st * expf(f1 - f2 * expf(f3 * ls + f4 * ls * ls));
+  const float ls = __logf(Splus);
+  return 2.0f * kPiF * effR * st * __expf(f1 - f2 * __expf(f3 * ls + f4 * ls * ls));
 }
 
 __device__ __forceinline__ MixedRec load_rec(const ContactRec* p) {
@@ -288,6 +292,16 @@ __device__ __forceinline__ void split_hi_lo(double xo, int dexp, float lo_scale,
   }
 }
 
+/* read-only global loads (inputs of the step: never written by this launch) */
+template <class T>
+__device__ __forceinline__ T ro(const T* p) {
+  return __ldg(p);
+}
+/* pull a line into L2 ahead of its use (no register is held meanwhile) */
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void warp_add(unsigned long long* ctr, unsigned v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -295,13 +309,19 @@ __device__ __forceinline__ void warp_add(unsigned long long* ctr, unsigned v) {
 }
 
 template <bool WET>
-__global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
+__global__ void __launch_bounds__(128, 5) k_step_mixed(MixArgs a) {
   if (a.n <= 0) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = q < a.n;
   const int qq = live ? q : a.n - 1;
+  /* the integrator's FP64 state is needed only after the pair loop: start
+   * bringing it in now */
+  prefetch_l2(a.pos + qq);
+  prefetch_l2(a.vel + qq);
+  prefetch_l2(a.angv + qq);
+  prefetch_l2(a.pmove + qq);
 
-  const float4 hi = a.phi_in[qq], lo = a.plo_in[qq], vi4 = a.v_in[qq], wi4 = a.w_in[qq];
+  const float4 hi = ro(a.phi_in + qq), lo = ro(a.plo_in + qq), vi4 = ro(a.v_in + qq), wi4 = ro(a.w_in + qq);
   const float ri = hi.w + lo.w;
   const float3 iv = f3(vi4.x, vi4.y, vi4.z), iw = f3(wi4.x, wi4.y, wi4.z);
   const float twor = 2.0f * ri;
@@ -316,15 +336,23 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
     if (inl < 12) inl = 12;
     iVol = a.lqd_vol * mass_f / (float)inl;
   }
-  const int L = a.plevel[qq];
-  const long long stride = a.npars[L];
-  const long long base = slot_base(L, a.npars, a.nneb) + a.nidx[qq];
-  const int nn = live ? a.num_nebor[qq] : 0;
+  const int L = ro(a.plevel + qq);
+  const long long stride = ro(a.npars + L);
+  const long long base = slot_base(L, a.npars, a.nneb) + ro(a.nidx + qq);
+  const int nn = live ? ro(a.num_nebor + qq) : 0;
   unsigned ncont = 0, nbr = 0;
+  /* one slot ahead: the next partner's index and coarse shadow are in flight
+   * while the current pair is evaluated */
+  int j_next = nn > 0 ? ro(a.nebor + base) : 0;
+  float4 hj_next = ro(a.phi_in + j_next);
   for (int k = 0; k < nn; k++) {
     const long long s = base + k * stride;
-    const int j = a.nebor[s];
-    const float4 hj = a.phi_in[j];
+    const int j = j_next;
+    const float4 hj = hj_next;
+    if (k + 1 < nn) {
+      j_next = ro(a.nebor + s + stride);
+      hj_next = ro(a.phi_in + j_next);
+    }
     const float ax = hi.x - hj.x, ay = hi.y - hj.y, az = hi.z - hj.z; /* exact */
     const float shi = hi.w + hj.w;
     const float coarse = sqrtf(ax * ax + ay * ay + az * az) - shi;
@@ -332,8 +360,10 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
     float3 u = f3(0.f, 0.f, 0.f);
     float rj = hj.w;
     const bool cand = WET || coarse < a.coarse_tol;
+    float4 vj4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (WET) vj4 = ro(a.v_in + j);
     if (cand) {
-      const float4 lj = a.plo_in[j];
+      const float4 lj = ro(a.plo_in + j);
       rj = hj.w + lj.w;
       const float bx = lo.x - lj.x, by = lo.y - lj.y, bz = lo.z - lj.z;
       /* d^2 - S^2 from exact pieces */
@@ -352,11 +382,12 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
       const float D = s3 + small;
       const float dx = ax + bx, dy = ay + by, dz = az + bz;
       const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
-      gap = D / (dist + (Sh + Sl));
-      const float inv = 1.0f / dist;
+      gap = __fdividef(D, dist + (Sh + Sl));
+      const float inv = __frcp_rn(dist);
       u = f3(dx * inv, dy * inv, dz * inv);
       if (gap < 0.f) {
-        const float4 vj4 = a.v_in[j], wj4 = a.w_in[j];
+        if (!WET) vj4 = ro(a.v_in + j);
+        const float4 wj4 = ro(a.w_in + j);
         const float3 jv = f3(vj4.x, vj4.y, vj4.z), jw = f3(wj4.x, wj4.y, wj4.z);
         const float3 cpv = (iv - jv) - crossf(iw * ri + jw * rj, u);
         const float ijRad = ri * rj / (ri + rj);
@@ -372,12 +403,12 @@ __global__ void __launch_bounds__(128) k_step_mixed(MixArgs a) {
       }
     }
     if (WET) {
-      int jnl = __float_as_int(a.v_in[j].w);
+      int jnl = __float_as_int(vj4.w);
       if (jnl < 12) jnl = 12;
       const float tj = 2.0f * rj;
-      const float jVol = a.lqd_vol * (tj * tj * tj) / (float)jnl;
+      const float jVol = __fdividef(a.lqd_vol * (tj * tj * tj), (float)jnl);
       float ijVol = iVol + jVol;
-      const float rupture = 0.99f * exp2f(0.33f * log2f(ijVol));
+      const float rupture = 0.99f * exp2f(0.33f * __log2f(ijVol));
       int b = a.brg[s];
       if (gap < 2.0f * a.lqd_layer * (ri + rj)) b = 1;
       else if (gap > rupture) b = 0;
@@ -547,6 +578,7 @@ Law32 make_law(const calParaPP& c, bool pp, double dmp_sq, int stage) {
   l.ystiff = (float)c.ystiff_t;
   l.rot_eps = pp ? 1.0e-7f : 1.0e-10f;
   l.dsmx_eps = pp ? 1.0e-7f : 1.0e-10f;
+  l.kt = (float)(16.0 * (1.0 - c.pois) * c.emod / (4.0 - 2.0 * c.pois));
   l.dmp = (float)std::sqrt(dmp_sq);
   l.hertz_le = pp ? 1 : 0;
   l.damp_on = pp ? (stage == 1) : (stage == 1 || stage == 7);
