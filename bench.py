@@ -179,6 +179,9 @@ def main():
                     help="untimed steps before the warm-up: gravity loads the deposited bed's contacts")
     ap.add_argument("--no-fp64-check", dest="fp64_check", action="store_false",
                     help="skip the FP64 rerun that gives the packing-fraction and coordination errors")
+    ap.add_argument("--capnet-samples", type=int, default=5_000_000,
+                    help="training samples for the learned capillary closure, logged while settling (0: skip it)")
+    ap.add_argument("--capnet-epochs", type=int, default=20)
     ap.add_argument("--ref-gpu-steps", type=int, default=40,
                     help="timed steps of the reference's own kernels on this GPU (0: skip)")
     ap.add_argument("--host-steps", action="store_true",
@@ -218,37 +221,60 @@ def main():
     eng.lib.dem_l2_flush.restype = C.c_int
     eng.lib.dem_l2_flush.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
 
-    def l2_flush():
-        check(eng.lib.dem_l2_flush(C.c_void_p(eng.stream()), C.c_void_p(flush.data_ptr()), flush.numel()),
+    def l2_flush(e):
+        """evict L2 on engine e's stream, so the eviction finishes before e's next step starts"""
+        check(e.lib.dem_l2_flush(C.c_void_p(e.stream()), C.c_void_p(flush.data_ptr()), flush.numel()),
               "dem_l2_flush")
 
-    eng.step(args.settle)
+    def timed_steps(e, steps, all_ranks=True):
+        """`steps` single steps of engine e, L2 evicted before each, CUDA events
+        on its stream around each step; returns (ms total, wall s, clocks, stats before, after)"""
+        st = torch.cuda.ExternalStream(e.stream())
+        e.sync()
+        before = e.stats()
+        clk = Clocks()
+        clk.start()
+        if ws > 1 and all_ranks:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        evs = []
+        for _ in range(steps):
+            l2_flush(e)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            e.step(1)
+            b.record(st)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        if ws > 1 and all_ranks:
+            torch.distributed.barrier()
+        wall = time.perf_counter() - t0
+        ckk = clk.stop(local)
+        e.sync()
+        return sum(a.elapsed_time(b) for a, b in evs), wall, ckk, before, e.stats()
+
+    # settle; the learned closure's training samples are logged from the formula
+    # engine along the way (outside every timed region)
+    from gpucode_gb300 import capnet as cn
+
+    use_net = rank == 0 and args.capnet_samples > 0 and not args.host_steps
+    n_snap = 11
+    per_snap = -(-args.capnet_samples // n_snap)
+    xs, ys = [], []
+    if use_net and args.settle >= 2 * n_snap:
+        first = args.settle - n_snap * (args.settle // (n_snap + 1))
+        eng.step(first)
+        for _ in range(n_snap):
+            eng.step(args.settle // (n_snap + 1))
+            x, y = cn.collect_samples(eng, per_snap)
+            xs.append(x.clone())
+            ys.append(y.clone())
+    else:
+        eng.step(args.settle)
     eng.step(args.warmup)
-    eng.sync()
-    s0 = eng.stats()
-    clocks = Clocks()
-    clocks.start()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    t_wall = time.perf_counter()
-    evs = []
-    for _ in range(args.steps):
-        l2_flush()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        eng.step(1)
-        b.record(stream)
-        evs.append((a, b))
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    t_wall = time.perf_counter() - t_wall
-    ck = clocks.stop(local)
-    eng.sync()
-    s1 = eng.stats()
-    ms = sum(a.elapsed_time(b) for a, b in evs)
+    ms, t_wall, ck, s0, s1 = timed_steps(eng, args.steps)
     steps_run = args.settle + args.warmup + args.steps
     pos_mixed = eng.get_state()["pos"]
     if ws > 1:
@@ -295,9 +321,10 @@ def main():
 
     # accuracy: the same bed, the same number of steps, all-FP64 reference formulas
     accuracy = None
-    if rank == 0 and args.fp64_check:
-        from gpucode_gb300.engine import packing_metrics
+    mr = None
+    from gpucode_gb300.engine import packing_metrics
 
+    if rank == 0 and args.fp64_check:
         ref = Engine(w.setup, precision="fp64", use_graph=True)
         ref.set_state(w.pos0_reduced)
         t0 = time.perf_counter()
@@ -312,6 +339,64 @@ def main():
                     "z_rel_err": abs(mm["z"] - mr["z"]) / max(mr["z"], 1e-300), "n_probe": mr["n_probe"],
                     "fp64_particle_steps_per_s": n * steps_run / t_fp64,
                     "max_position_diff": float(np.abs(pos_mixed - pos_ref).max())}
+
+    # the learned capillary closure: trained on the logged samples by the
+    # library's own kernels, then the same bed stepped from the start with the
+    # network fused into the step kernel (BF16 tensor-core tiles)
+    closure = None
+    if use_net and xs:
+        x = torch.cat(xs).contiguous()
+        y = torch.cat(ys).contiguous()
+        xs, ys = [], []
+        net = cn.CapNet(seed=0)
+        rep = net.fit(x, y, epochs=args.capnet_epochs, batch=8192, lr=1e-3, val_frac=0.1, seed=2024)
+        em = Engine(w.setup, precision="mixed", capillary="mlp", graph_steps=1)
+        em.set_capnet(net)
+        em.set_state(w.pos0_reduced)
+        em.step(args.settle + args.warmup)
+        ms_m, _, ck_m, m0, m1 = timed_steps(em, args.steps, all_ranks=False)
+        value_m = n * args.steps / (ms_m / 1000.0)
+        ms_km = C.c_double()
+        check(em.lib.dem_profile_step(em.h, args.profile_reps, C.c_void_p(flush.data_ptr()), flush.numel(),
+                                      C.byref(ms_km)), "dem_profile_step")
+        pos_m = em.get_state()["pos"]
+        evals, falls = m1["cap_mlp"] - m0["cap_mlp"], m1["cap_fallback"] - m0["cap_fallback"]
+        em.close()
+
+        def per_call_ms(fn, reps=5):
+            fn()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                fn()
+            b.record()
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / reps
+
+        big = x[: min(len(x), 2_000_000)].contiguous()
+        nb = len(big)
+        rates = {"network_bf16_tensor_cores": nb / per_call_ms(lambda: net.infer(big, True)) * 1e3,
+                 "network_fp32": nb / per_call_ms(lambda: net.infer(big, False)) * 1e3,
+                 "formula_fp64_as_reference": nb / per_call_ms(lambda: cn.formula(big, True)) * 1e3,
+                 "formula_fp32_step_kernel": nb / per_call_ms(lambda: cn.formula(big, False)) * 1e3}
+        net.close()
+        closure = {"value": value_m, "unit": UNIT, "ms_per_step": ms_m / args.steps, "kernel_ms": ms_km.value,
+                   "clocks": ck_m, "samples": len(x), "epochs": rep["epochs"], "fit_seconds": rep["seconds"],
+                   "val_mse_standardised": rep["val_mse"], "val_force_rel_err_mean": rep["val_force_rel_mean"],
+                   "val_force_rel_err_max": rep["val_force_rel_max"],
+                   "val_rupture_rel_err_max": rep["val_rupture_rel_max"],
+                   "rebuilds": m1["rebuilds"] - m0["rebuilds"],
+                   "network_evaluations_per_step": evals / args.steps,
+                   "formula_fallback_fraction": falls / max(evals + falls, 1),
+                   "evaluations_per_s": rates}
+        mmlp = packing_metrics(w.setup, pos_m)
+        closure["phi"] = mmlp["phi"]
+        closure["z"] = mmlp["z"]
+        if mr is not None:
+            closure["phi_rel_err_vs_fp64"] = abs(mmlp["phi"] - mr["phi"]) / mr["phi"]
+            closure["z_rel_err_vs_fp64"] = abs(mmlp["z"] - mr["z"]) / max(mr["z"], 1e-300)
+        del x, y, big
 
     # the reference's own kernels (kernel.cu built for sm_103a) on this GPU, same bed
     ref_gpu = None
@@ -332,6 +417,7 @@ def main():
                                          "UpdateSystemG": r["update_ms"]},
                            "rebuilds": r["rebuilds"], "slot_overflow": bool(r["overflow"]),
                            "speedup": value / rv,
+                           "speedup_with_learned_closure": closure["value"] / rv if closure else None,
                            "kernel_speedup": (r["force_ms"] + r["wall_ms"] + r["update_ms"]) / ms_k.value,
                            "sample": f"{args.ref_gpu_steps} steps after 5 warm-up from this bed's final state, "
                                      "histories empty, L2 evicted before each step, main.cpp step order "
@@ -369,6 +455,7 @@ def main():
             "clocks": ck,
             "accuracy_vs_fp64": accuracy,
             "reference_kernels_gpu": ref_gpu,
+            "learned_closure": closure,
         }
         print(json.dumps(line), flush=True)
     eng.close()

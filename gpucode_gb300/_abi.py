@@ -127,7 +127,19 @@ class DemOptions(C.Structure):
 class DemStats(C.Structure):
     _fields_ = [("iter", C.c_longlong), ("rebuilds", C.c_longlong), ("nb_entries", C.c_longlong),
                 ("contacts", C.c_longlong), ("bridges", C.c_longlong), ("wall_contacts", C.c_longlong),
-                ("error_bits", C.c_int), ("pad", C.c_int), ("ctime", C.c_double)]
+                ("error_bits", C.c_int), ("pad", C.c_int), ("ctime", C.c_double), ("cap_mlp", C.c_longlong),
+                ("cap_fallback", C.c_longlong)]
+
+
+class CapnetFitOpts(C.Structure):
+    _fields_ = [("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_float), ("val_frac", C.c_float),
+                ("seed", C.c_ulonglong)]
+
+
+class CapnetReport(C.Structure):
+    _fields_ = [("epochs", C.c_int), ("n_train", C.c_int), ("n_val", C.c_int), ("pad", C.c_int),
+                ("train_mse", C.c_float * 64), ("val_mse", C.c_float), ("val_force_rel_mean", C.c_float),
+                ("val_force_rel_max", C.c_float), ("val_rupture_rel_max", C.c_float), ("seconds", C.c_double)]
 
 
 # expected C layout, in the order dem_abi_layout reports it
@@ -200,6 +212,17 @@ def _declare(lib: C.CDLL) -> None:
         "dem_packing_metrics": (I, [I, P, P, P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(I)]),
         "dem_l2_flush": (I, [P, P, C.c_size_t]),
         "dem_compat_errors": (I, []),
+        "dem_capnet_create": (I, [C.c_ulonglong, C.POINTER(P)]),
+        "dem_capnet_destroy": (None, [P]),
+        "dem_capnet_get": (I, [P, P, P]),
+        "dem_capnet_set": (I, [P, P, P]),
+        "dem_capnet_samples": (I, [P, P, P, C.c_longlong, C.POINTER(C.c_longlong)]),
+        "dem_capnet_fit": (I, [P, P, P, C.c_longlong, C.POINTER(CapnetFitOpts), C.POINTER(CapnetReport)]),
+        "dem_capnet_grad": (I, [P, P, P, I, P, P]),
+        "dem_capnet_infer": (I, [P, P, C.c_longlong, I, P]),
+        "dem_capnet_formula": (I, [P, C.c_longlong, I, P]),
+        "dem_set_capnet": (I, [P, P]),
+        "dem_set_contact_angles": (I, [P, C.c_float, C.c_ulonglong]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -33,6 +33,7 @@ UNITS = [
     ("compat.cu", []),
     ("engine.cu", []),
     ("mixed.cu", []),
+    ("capnet.cu", []),
 ]
 
 

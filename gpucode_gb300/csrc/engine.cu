@@ -439,11 +439,18 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
     delete c;
     return fail(DEM_ERR_ARG, "dem_create: the mixed-precision path needs reorder = 1");
   }
+  if (c->opt.capillary == DEM_CAP_MLP && c->opt.precision != DEM_PREC_MIXED) {
+    delete c;
+    return fail(DEM_ERR_ARG, "dem_create: the learned capillary closure runs on the mixed-precision path only");
+  }
   c->n = s->np;
   c->slots = s->n_pp_slots;
   c->mx = nullptr;
   c->graph_exec[0] = c->graph_exec[1] = nullptr;
   c->parity = 0;
+  c->cap_w = nullptr;
+  c->theta_max = 0.52359878f; /* 30 degrees */
+  c->theta_seed = 0;
   c->iter = 0;
   c->ctime = 0.0;
   std::memcpy(c->k.mat, s->mat, sizeof(c->k.mat));
@@ -720,6 +727,8 @@ extern "C" dem_status dem_get_stats(dem_ctx* c, dem_stats* st) {
   st->wall_contacts = (long long)ctr[3];
   st->error_bits = err;
   st->ctime = c->ctime;
+  st->cap_mlp = (long long)ctr[5];
+  st->cap_fallback = (long long)ctr[6];
   return DEM_OK;
 }
 

@@ -80,6 +80,11 @@ struct dem_ctx {
   /* CUDA graphs of opt.graph_steps steps, one per starting shadow parity */
   cudaGraphExec_t graph_exec[2];
   int parity; /* mixed: which shadow buffer the next step reads */
+  /* learned capillary closure (DEM_CAP_MLP): the staged network on the device
+   * (NULL until dem_set_capnet) and the particles' contact angles */
+  void* cap_w;
+  float theta_max;
+  unsigned long long theta_seed;
 };
 
 namespace dem {

@@ -35,6 +35,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "capnet.cuh"
 #include "dem_device.cuh"
 #include "engine.h"
 
@@ -88,6 +89,11 @@ struct MixArgs {
   float dtf, coarse_tol, rfrc;
   float lqd_vol, lqd_layer, lqd_gapmn, lqd_st;
   Law32 pp, pw;
+  /* learned capillary closure (NET variant only) */
+  const int* id;
+  const CapNetSmem* capw;
+  unsigned long long theta_seed;
+  float theta_max;
 };
 
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
@@ -243,19 +249,9 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
   r.stage = st;
 }
 
-/* kernel.cu:65-81 in FP32.  The hardware approximations of log and exp are
- * used: their errors (a few ulp, relative) stay far below the FP32 force
- * tolerance, and the regression they feed is itself a fit. */
+/* kernel.cu:65-81 in FP32 (the normalised regression: capnet.cuh) */
 __device__ __forceinline__ float fcap32(float Splus, float ijVol, float effR, float gapmn, float st) {
-  Splus = fmaxf(gapmn, Splus);
-  Splus = Splus * rsqrtf(ijVol);
-  const float L = __logf(ijVol), L2 = L * L, L3 = L2 * L;
-  const float f1 = -0.44507f - 0.1119f * L - 0.012101f * L2 - 0.0005f * L3;
-  const float f2 = 1.9222f - 0.0668f * L - 0.0013375f * L2;
-  const float f3 = 1.268f + 0.198f * L + 0.02232f * L2 + 0.0008585f * L3;
-  const float f4 = -0.010703f + 0.03345f * L + 0.0018574f * L2;
-  const float ls = __logf(Splus);
-  return 2.0f * kPiF * effR * st * __expf(f1 - f2 * __expf(f3 * ls + f4 * ls * ls));
+  return 2.0f * kPiF * effR * st * cap_formula32(fmaxf(gapmn, Splus), ijVol);
 }
 
 __device__ __forceinline__ MixedRec load_rec(const ContactRec* p) {
@@ -308,12 +304,90 @@ __device__ __forceinline__ void warp_add(unsigned long long* ctr, unsigned v) {
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(ctr, (unsigned long long)v);
 }
 
-template <bool WET>
-__global__ void __launch_bounds__(128, 5) k_step_mixed(MixArgs a) {
+/* One bridge waiting for the learned closure: 40 bytes in a per-warp queue in
+ * shared memory.  After the network has run, sep and vol hold its two outputs
+ * (normalised force, rupture distance). */
+struct CapEntry {
+  float sep, vol, theta, ratio; /* raw features */
+  float wx, wy, wz;             /* -2 pi R_eff gamma u: the force per unit normalised force */
+  float gap;
+  unsigned slot;
+  int meta; /* bit 0: the bridge forms this step (gap below the liquid layer); bits 8..: 1 + the
+               queue index of the same lane's previous entry (0: none) */
+};
+constexpr int kCapQ = 128; /* entries per warp; flushed before an iteration could overflow it */
+#ifndef DEM_NET_BLOCKS
+#define DEM_NET_BLOCKS 4
+#endif
+/* resident blocks per SM the network variant is built for: 4 (no register
+ * spills) measured faster than 5 on the 200k wet bed */
+constexpr int kNetBlocks = DEM_NET_BLOCKS;
+constexpr int kWarps = 4;  /* warps per block of the step kernel */
+constexpr size_t kCapSmem = ((sizeof(CapNetSmem) + 15) / 16) * 16 + sizeof(CapEntry) * kCapQ * kWarps;
+
+__device__ __forceinline__ uint32_t cap_pair(const CapNetSmem& w, const CapEntry& e, int t) {
+  return cap_pair(w, e.sep, e.vol, e.theta, e.ratio, t);
+}
+
+/* Run the queued bridges of this warp through the network (16-row BF16
+ * tensor-core tiles), then let every lane fold in its own bridges, walking
+ * its chain of entries from the newest: rupture decision, bridge flag,
+ * force.  All 32 lanes call it; `last` is the lane's newest entry (-1: none). */
+__device__ __forceinline__ void cap_flush(const CapNetSmem& w, CapEntry* qw, int qn, int last, unsigned char* brg,
+                                          KSum3& F, int& wet, unsigned& nbr, unsigned& nmlp) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  __syncwarp();
+  for (int t0 = 0; t0 < qn; t0 += 16) {
+    const int r0 = t0 + g, r1 = r0 + 8;
+    uint32_t xa = 0u, xb = 0u;
+    if (t < 2) {
+      if (r0 < qn) xa = cap_pair(w, qw[r0], t);
+      if (r1 < qn) xb = cap_pair(w, qw[r1], t);
+    }
+    float o[4];
+    cap_tile16(w, xa, xb, o);
+    __syncwarp();
+    if (t == 0) {
+      if (r0 < qn) {
+        qw[r0].sep = o[0] * w.y_std[0] + w.y_mean[0];
+        qw[r0].vol = o[1] * w.y_std[1] + w.y_mean[1];
+      }
+      if (r1 < qn) {
+        qw[r1].sep = o[2] * w.y_std[0] + w.y_mean[0];
+        qw[r1].vol = o[3] * w.y_std[1] + w.y_mean[1];
+      }
+    }
+    __syncwarp();
+  }
+  for (int e = last; e >= 0;) {
+    const CapEntry& en = qw[e];
+    e = (en.meta >> 8) - 1;
+    const int b = (en.meta & 1) ? 1 : (en.gap > en.vol ? 0 : 1);
+    brg[en.slot] = (unsigned char)b;
+    nmlp++;
+    if (b) {
+      F.add(f3(en.wx, en.wy, en.wz) * en.sep);
+      wet++;
+      if (en.gap >= 0.f) nbr++;
+    }
+  }
+  __syncwarp();
+}
+
+template <bool WET, bool NET>
+__global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArgs a) {
   if (a.n <= 0) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = q < a.n;
   const int qq = live ? q : a.n - 1;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const CapNetSmem* capw = reinterpret_cast<const CapNetSmem*>(dsm);
+  CapEntry* qw = reinterpret_cast<CapEntry*>(dsm + ((sizeof(CapNetSmem) + 15) / 16) * 16) +
+                 (threadIdx.x >> 5) * kCapQ;
+  if (NET) {
+    cap_stage(a.capw, reinterpret_cast<CapNetSmem*>(dsm));
+    __syncthreads();
+  }
   /* the integrator's FP64 state is needed only after the pair loop: start
    * bringing it in now */
   prefetch_l2(a.pos + qq);
@@ -340,12 +414,22 @@ __global__ void __launch_bounds__(128, 5) k_step_mixed(MixArgs a) {
   const long long stride = ro(a.npars + L);
   const long long base = slot_base(L, a.npars, a.nneb) + ro(a.nidx + qq);
   const int nn = live ? ro(a.num_nebor + qq) : 0;
-  unsigned ncont = 0, nbr = 0;
+  unsigned ncont = 0, nbr = 0, nmlp = 0, nfall = 0;
+  /* learned closure: the warp walks its lanes' slots in lockstep so that
+   * bridges can be queued and evaluated 16 at a time on the tensor cores */
+  const int lane = threadIdx.x & 31;
+  const int nloop = NET ? __reduce_max_sync(0xffffffffu, nn) : nn;
+  const float th_i = NET ? cap_theta(ro(a.id + qq), a.theta_seed, a.theta_max) : 0.f;
+  int qn = 0;    /* entries in this warp's queue (warp-uniform) */
+  int last = -1; /* this lane's newest entry in it */
   /* one slot ahead: the next partner's index and coarse shadow are in flight
    * while the current pair is evaluated */
   int j_next = nn > 0 ? ro(a.nebor + base) : 0;
   float4 hj_next = ro(a.phi_in + j_next);
-  for (int k = 0; k < nn; k++) {
+  for (int k = 0; k < nloop; k++) {
+    bool want = false; /* NET: this lane queues `ent` at the end of the iteration */
+    CapEntry ent;
+    if (!NET || k < nn) { /* the slot body (lanes with a k-th neighbour) */
     const long long s = base + k * stride;
     const int j = j_next;
     const float4 hj = hj_next;
@@ -408,20 +492,64 @@ __global__ void __launch_bounds__(128, 5) k_step_mixed(MixArgs a) {
       const float tj = 2.0f * rj;
       const float jVol = __fdividef(a.lqd_vol * (tj * tj * tj), (float)jnl);
       float ijVol = iVol + jVol;
-      const float rupture = 0.99f * exp2f(0.33f * __log2f(ijVol));
-      int b = a.brg[s];
-      if (gap < 2.0f * a.lqd_layer * (ri + rj)) b = 1;
-      else if (gap > rupture) b = 0;
-      a.brg[s] = (unsigned char)b;
-      if (b) {
+      const int bprev = a.brg[s];
+      const bool form = gap < 2.0f * a.lqd_layer * (ri + rj);
+      if (NET && (bprev || form)) {
+        /* a bridge to evaluate: queue it for the network, or (outside the
+         * network's training box) take the plain formula right here */
+        const float sep = fmaxf(a.lqd_gapmn, fmaxf(gap, 0.f)), vol = 8.0f * ijVol;
+        const float theta = 0.5f * (th_i + cap_theta(ro(a.id + j), a.theta_seed, a.theta_max));
+        const float ratio = __fdividef(fminf(ri, rj), fmaxf(ri, rj));
         const float effR = 2.0f * ri * rj / (ri + rj);
-        const float fc = fcap32(gap < 0.f ? 0.f : gap, ijVol * 8.0f, effR, a.lqd_gapmn, a.lqd_st);
-        F.add(u * (-fc));
-        wet++;
-        if (gap >= 0.f) nbr++;
+        if (cap_in_hull(*capw, sep, vol, theta, ratio) && s <= 0xffffffffLL) {
+          const float3 wv = u * (-2.0f * kPiF * effR * a.lqd_st);
+          ent = CapEntry{sep, vol, theta, ratio, wv.x, wv.y, wv.z, gap, (unsigned)s, form ? 1 : 0};
+          want = true;
+        } else {
+          const float rupture = 0.99f * exp2f(0.33f * __log2f(ijVol));
+          const int b = form ? 1 : (gap > rupture ? 0 : 1);
+          a.brg[s] = (unsigned char)b;
+          if (b) {
+            const float fc = fcap32(gap < 0.f ? 0.f : gap, vol, effR, a.lqd_gapmn, a.lqd_st);
+            F.add(u * (-fc));
+            wet++;
+            if (gap >= 0.f) nbr++;
+          }
+          nfall++;
+        }
+      } else if (!NET) {
+        const float rupture = 0.99f * exp2f(0.33f * __log2f(ijVol));
+        int b = bprev;
+        if (form) b = 1;
+        else if (gap > rupture) b = 0;
+        a.brg[s] = (unsigned char)b;
+        if (b) {
+          const float effR = 2.0f * ri * rj / (ri + rj);
+          const float fc = fcap32(gap < 0.f ? 0.f : gap, ijVol * 8.0f, effR, a.lqd_gapmn, a.lqd_st);
+          F.add(u * (-fc));
+          wet++;
+          if (gap >= 0.f) nbr++;
+        }
+      }
+    }
+    }
+    if (NET) {
+      const unsigned m = __ballot_sync(0xffffffffu, want);
+      if (want) {
+        const int pos = qn + __popc(m & ((1u << lane) - 1u));
+        ent.meta |= (last + 1) << 8;
+        qw[pos] = ent;
+        last = pos;
+      }
+      qn += __popc(m);
+      if (qn > kCapQ - 32) {
+        cap_flush(*capw, qw, qn, last, a.brg, F, wet, nbr, nmlp);
+        qn = 0;
+        last = -1;
       }
     }
   }
+  if (NET && qn > 0) cap_flush(*capw, qw, qn, last, a.brg, F, wet, nbr, nmlp);
 
   /* cylinder walls (CirPWInterG), geometry in FP64 */
   unsigned nwc = 0;
@@ -530,6 +658,10 @@ __global__ void __launch_bounds__(128, 5) k_step_mixed(MixArgs a) {
     warp_add(&a.counters[1], ncont);
     warp_add(&a.counters[2], nbr);
     warp_add(&a.counters[3], nwc);
+    if (NET) {
+      warp_add(&a.counters[5], nmlp);
+      warp_add(&a.counters[6], nfall);
+    }
   }
 }
 
@@ -668,11 +800,19 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   calParaPP pw;
   std::memcpy(&pw, &c->s.pwcal, sizeof(pw));
   a.pw = make_law(pw, false, c->s.mat[0].dmpn * c->s.mat[1].dmpn, c->s.load_stage);
-  const int bs = 128;
-  if (c->s.force_cap == 1)
-    k_step_mixed<true><<<grid_for(c->n, bs), bs, 0, s>>>(a);
-  else
-    k_step_mixed<false><<<grid_for(c->n, bs), bs, 0, s>>>(a);
+  a.id = b.id;
+  a.capw = reinterpret_cast<const CapNetSmem*>(c->cap_w);
+  a.theta_seed = c->theta_seed;
+  a.theta_max = c->theta_max;
+  const int bs = 32 * kWarps;
+  if (c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP) {
+    if (!c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
+    k_step_mixed<true, true><<<grid_for(c->n, bs), bs, kCapSmem, s>>>(a);
+  } else if (c->s.force_cap == 1) {
+    k_step_mixed<true, false><<<grid_for(c->n, bs), bs, 0, s>>>(a);
+  } else {
+    k_step_mixed<false, false><<<grid_for(c->n, bs), bs, 0, s>>>(a);
+  }
   return cuda_check(cudaGetLastError(), "mixed_step launch");
 }
 

@@ -132,6 +132,14 @@ class Engine:
         check(self.lib.dem_get_history(self.h, ptr(rec), ptr(brg), max_per), "dem_get_history")
         return rec, brg
 
+    # ---- learned capillary closure ----
+    def set_capnet(self, net) -> None:
+        """install a trained CapNet (the engine must use capillary="mlp")"""
+        check(self.lib.dem_set_capnet(self.h, net.h), "dem_set_capnet")
+
+    def set_contact_angles(self, theta_max_rad: float, seed: int = 0) -> None:
+        check(self.lib.dem_set_contact_angles(self.h, float(theta_max_rad), int(seed)), "dem_set_contact_angles")
+
     def save(self, path: str | os.PathLike, nbatch: int = 1) -> None:
         check(self.lib.dem_save(self.h, str(path).encode(), nbatch), "dem_save")
 

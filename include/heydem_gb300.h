@@ -276,6 +276,8 @@ typedef struct dem_stats {
   int error_bits;         /* device error word (1: overflow, 2: non-finite, 4: cell range) */
   int pad;
   double ctime;           /* simulated time (reduced) */
+  long long cap_mlp;      /* DEM_CAP_MLP: bridges evaluated by the network (cumulative) */
+  long long cap_fallback; /* DEM_CAP_MLP: bridges outside its training box, plain formula (cumulative) */
 } dem_stats;
 
 void dem_default_options(dem_options* o);
@@ -376,6 +378,65 @@ dem_status dem_pack_deposit(int n, const double* dia, double cx, double cy, doub
  * p-p contacts of the spheres centred in the probe. */
 dem_status dem_packing_metrics(int n, const double3* pos, const double* rad, const CylinderBC* cyl, double* phi,
                                double* z_mean, int* n_probe);
+/* ---- learned capillary closure (no counterpart in the reference) ----
+ * A 4 -> 64 -> 64 -> 2 SiLU network standing in for the reference's capillary
+ * routine fCap (kernel.cu:65-81) and rupture distance (kernel.cu:518).
+ * Raw features per bridge, in the reduced length unit of the kernels:
+ *   [0] S+ = max(gapmn, gap)  [1] V = 8 (Vi + Vj)  [2] contact angle [rad]
+ *   [3] radius ratio r_min / r_max
+ * raw targets: [0] F / (2 pi R_eff gamma)  [1] rupture distance 0.99 (V/8)^0.33.
+ * Parameter vector (FP32, 4610): W1[64][4] b1[64] W2[64][64] b2[64] W3[2][64] b3[2];
+ * standardisation vector (20): x_mean[4] x_std[4] y_mean[2] y_std[2], and the
+ * training box of the raw features hull_lo[4] hull_hi[4]. */
+typedef struct dem_capnet dem_capnet;
+typedef struct dem_capnet_fit_opts {
+  int epochs;             /* passes over the training split */
+  int batch;              /* samples per Adam step */
+  float lr;               /* Adam learning rate (beta 0.9 / 0.999, eps 1e-8) */
+  float val_frac;         /* held-out fraction (seeded split) */
+  unsigned long long seed;
+} dem_capnet_fit_opts;
+typedef struct dem_capnet_report {
+  int epochs, n_train, n_val, pad;
+  float train_mse[64];    /* standardised MSE per epoch (sampled batches), first 64 epochs */
+  float val_mse;          /* standardised MSE of the FP32 network on the held-out split */
+  float val_force_rel_mean, val_force_rel_max; /* BF16 tensor-core network vs the formula's force */
+  float val_rupture_rel_max;
+  double seconds;
+} dem_capnet_report;
+
+dem_status dem_capnet_create(unsigned long long seed, dem_capnet** out);
+void dem_capnet_destroy(dem_capnet* net);
+/* parameters (4610) and standardisation (20), host arrays; either may be NULL */
+dem_status dem_capnet_get(const dem_capnet* net, float* params, float* norm);
+dem_status dem_capnet_set(dem_capnet* net, const float* params, const float* norm);
+/* Training samples from a wet context's current state: every bridged pair,
+ * features x_dev[n][4] and the formula's targets y_dev[n][2] (FP64 formula,
+ * stored FP32), device arrays, in particle / slot order.  *count = samples
+ * written (at most capacity). */
+dem_status dem_capnet_samples(dem_ctx* c, float* x_dev, float* y_dev, long long capacity, long long* count);
+/* Adam on the network's own training kernels: seeded split, standardisation
+ * and training box from the training split, then validation. */
+dem_status dem_capnet_fit(dem_capnet* net, const float* x_dev, const float* y_dev, long long n,
+                          const dem_capnet_fit_opts* opt, dem_capnet_report* rep);
+/* Gradient of the loss (mean over the n samples of the squared error of the
+ * standardised outputs) with respect to the 4610 parameters, and the loss. */
+dem_status dem_capnet_grad(dem_capnet* net, const float* x_dev, const float* y_dev, int n, float* grad,
+                           float* loss);
+/* Raw features -> raw outputs: tensor_cores = 1 runs the BF16 tiles the step
+ * kernel uses, 0 the FP32 network. */
+dem_status dem_capnet_infer(dem_capnet* net, const float* x_dev, long long n, int tensor_cores, float* y_dev);
+/* The plain closure the network stands in for, on the same raw features:
+ * fp64 = 1 as the reference evaluates it (FP64 pow/log/exp), 0 the step
+ * kernel's FP32 form. */
+dem_status dem_capnet_formula(const float* x_dev, long long n, int fp64, float* y_dev);
+/* Install a trained network in a context created with DEM_PREC_MIXED and
+ * DEM_CAP_MLP; bridges outside its training box keep the plain formula. */
+dem_status dem_set_capnet(dem_ctx* c, dem_capnet* net);
+/* Contact angles: uniform in [0, theta_max] per particle, hashed from the
+ * particle id with `seed` (default 30 degrees, seed 0). */
+dem_status dem_set_contact_angles(dem_ctx* c, float theta_max, unsigned long long seed);
+
 /* Struct sizes and offsets of this header, for binding checks. */
 int dem_abi_layout(long long* out, int cap);
 

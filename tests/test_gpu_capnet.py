@@ -1,0 +1,217 @@
+"""The learned capillary closure on the GPU (dem_capnet_*, DEM_CAP_MLP) against
+the CPU oracle (oracle/mlp_oracle.py) and the plain formula it stands in for
+(kernel.cu:65-81, :518).
+
+Tolerances: FP32 training kernels vs the FP64 oracle 1e-4 of the largest
+gradient; FP32 inference 1e-4 (standardised outputs); BF16 tensor-core tiles vs
+the oracle's BF16 emulation 2e-2 worst / 2e-3 mean (standardised outputs: the
+emulation rounds with exact log/exp where the tiles use the hardware ones, so
+an activation can land on the other side of a BF16 rounding step)."""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import _workloads
+from gpucode_gb300 import capnet
+from gpucode_gb300.capnet import CapNet
+from gpucode_gb300.engine import Engine
+
+sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle"))
+import mlp_oracle as mo  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _random_features(rng, n):
+    x = np.column_stack([np.exp(rng.uniform(np.log(5e-6), np.log(0.05), n)),
+                         np.exp(rng.uniform(np.log(1e-4), np.log(0.05), n)),
+                         rng.uniform(0, 0.52, n), rng.uniform(0.25, 1.0, n)]).astype(np.float32)
+    y = mo.formula(x).astype(np.float32)
+    f = np.column_stack([np.log(x[:, 0].astype(np.float64)), np.log(x[:, 1].astype(np.float64)), x[:, 2], x[:, 3]])
+    norm = np.zeros(20, np.float32)
+    norm[0:4], norm[4:8] = f.mean(0), f.std(0)
+    norm[8:10], norm[10:12] = y.mean(0), y.std(0)
+    norm[12:16], norm[16:20] = x.min(0), x.max(0)
+    return x, y, norm
+
+
+def _t(a):
+    import torch
+
+    return torch.tensor(np.ascontiguousarray(a, np.float32), device="cuda")
+
+
+def test_training_gradient_matches_the_oracle(cuda):
+    rng = np.random.default_rng(11)
+    x, y, norm = _random_features(rng, 700)  # 6 blocks of 128, the last one partial
+    net = CapNet(seed=3)
+    net.set(norm=norm)
+    p, _ = net.get()
+    g, loss = net.grad(_t(x), _t(y))
+    lo, go = mo.loss_and_grad(p.astype(np.float64), x, y, norm.astype(np.float64))
+    assert abs(loss - lo) <= 1e-5 * lo, (loss, lo)
+    err = np.abs(g - go).max() / np.abs(go).max()
+    assert err < 1e-4, err
+    net.close()
+
+
+def test_inference_matches_the_oracle(cuda):
+    rng = np.random.default_rng(12)
+    x, y, norm = _random_features(rng, 5000)
+    net = CapNet(seed=4)
+    p = mo.init_params(9).astype(np.float32)
+    net.set(p, norm)
+    ys = norm[10:12].astype(np.float64)
+    want32, _ = mo.forward(p.astype(np.float64), mo.std_inputs(x, norm.astype(np.float64)))
+    got32 = net.infer(_t(x), tensor_cores=False).cpu().numpy()
+    assert np.abs((got32 - norm[8:10]) / ys - want32).max() < 1e-4
+    got = net.infer(_t(x), tensor_cores=True).cpu().numpy()
+    emul = mo.forward_bf16(p, x, norm.astype(np.float64))
+    d = np.abs(got - emul) / ys
+    assert d.max() < 2e-2 and d.mean() < 2e-3, (d.max(), d.mean())
+    # ragged tail: a count that is not a multiple of the 16-row tile
+    got_t = net.infer(_t(x[:37]), tensor_cores=True).cpu().numpy()
+    np.testing.assert_array_equal(got_t, got[:37])
+    net.close()
+
+
+def _wet_engine(steps, capillary="formula"):
+    w = _workloads.small_wet()
+    pos, vel, ang = _workloads.stirred(w, vscale=0.05, wscale=0.1)
+    eng = Engine(w.setup, precision="mixed", capillary=capillary)
+    eng.set_state(pos, vel, ang)
+    if steps:
+        eng.step(steps)
+    return w, eng, (pos, vel, ang)
+
+
+def test_samples_are_the_bridges_and_the_formula(cuda):
+    w, eng, _ = _wet_engine(30)
+    x, y = capnet.collect_samples(eng, 200_000)
+    xs, ys = x.cpu().numpy(), y.cpu().numpy()
+    _, brg = eng.history()
+    assert len(xs) == int((brg == 1).sum()) > 100
+    want = mo.formula(xs)
+    d = np.abs(ys - want) / np.abs(want)
+    assert d[:, 0].max() < 1e-5 and d[:, 1].max() < 1e-5, d.max(axis=0)
+    assert (xs[:, 0] >= w.setup.s.lqd.gapmn * (1 - 1e-6)).all()
+    assert ((xs[:, 2] >= 0) & (xs[:, 2] <= 0.5236)).all() and ((xs[:, 3] > 0) & (xs[:, 3] <= 1)).all()
+    f64 = capnet.formula(x, fp64=True).cpu().numpy()
+    f32 = capnet.formula(x, fp64=False).cpu().numpy()
+    assert np.abs(f64 - ys).max() <= 1e-6 * np.abs(ys).max()
+    assert (np.abs(f32 - ys) / np.abs(ys)).max() < 1e-4
+    eng.close()
+
+
+@pytest.fixture(scope="module")
+def trained(cuda):
+    """a network trained on bridges logged from a stirred wet bed"""
+    import torch
+
+    w, eng, _ = _wet_engine(0)
+    xs, ys = [], []
+    for _ in range(12):
+        eng.step(15)
+        x, y = capnet.collect_samples(eng, 200_000)
+        xs.append(x.clone())
+        ys.append(y.clone())
+    eng.close()
+    x, y = torch.cat(xs).contiguous(), torch.cat(ys).contiguous()
+    net = CapNet(seed=0)
+    rep = net.fit(x, y, epochs=60, batch=256, lr=3e-3, val_frac=0.1, seed=1)
+    return net, rep, x, y
+
+
+def test_training_learns_the_closure(trained):
+    net, rep, x, y = trained
+    assert rep["n_train"] + rep["n_val"] == len(x) and rep["n_val"] > 100
+    # what training gains: the same architecture and standardisation, untrained
+    fresh = CapNet(seed=0)
+    _, nz = net.get()
+    fresh.set(norm=nz)
+    _, mse0 = fresh.grad(x, y)
+    _, mse1 = net.grad(x, y)
+    assert mse1 < 0.02 * mse0, (mse1, mse0)
+    assert rep["val_mse"] < 0.02 * mse0
+    assert rep["val_force_rel_mean"] < 0.05, rep
+    assert rep["train_mse"][-1] < rep["train_mse"][0]
+    fresh.close()
+
+
+def test_network_gains_over_the_reference_precision_formula(trained):
+    """the trained network on the tensor cores against the plain closure as the
+    reference evaluates it (FP64 pow/log/exp): same inputs, time per bridge"""
+    import torch
+
+    net, _, x, _ = trained
+    big = x.repeat((2_000_000 // len(x)) + 1, 1)[:2_000_000].contiguous()
+    y_tc = net.infer(big, tensor_cores=True)
+    y_64 = capnet.formula(big, fp64=True)
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    t_tc = timed(lambda: net.infer(big, tensor_cores=True))
+    t_64 = timed(lambda: capnet.formula(big, fp64=True))
+    assert t_tc < 0.5 * t_64, (t_tc, t_64)
+    rel = (torch.abs(y_tc[:, 0] - y_64[:, 0]) / torch.abs(y_64[:, 0])).mean().item()
+    assert rel < 0.05
+
+
+def test_engine_with_an_empty_training_box_is_the_formula_engine(cuda):
+    """a network whose training box holds nothing sends every bridge to the
+    plain formula: the learned-closure kernel variant must then reproduce the
+    formula kernel bit for bit"""
+    w, ref, st = _wet_engine(0)
+    _, eng, _ = _wet_engine(0, capillary="mlp")
+    rng = np.random.default_rng(1)
+    _, _, norm = _random_features(rng, 100)
+    norm[12:16], norm[16:20] = 1.0, -1.0  # lo > hi: empty box
+    net = CapNet(seed=0)
+    net.set(norm=norm)
+    eng.set_capnet(net)
+    for e in (ref, eng):
+        e.step(40)
+    a, b = ref.get_state(), eng.get_state()
+    for k in ("pos", "vel", "angvel", "force"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    s = eng.stats()
+    assert s["cap_mlp"] == 0 and s["cap_fallback"] > 0
+    for e in (ref, eng):
+        e.close()
+    net.close()
+
+
+def test_engine_with_the_trained_network_tracks_the_formula(trained):
+    net, _, _, _ = trained
+    w, ref, st = _wet_engine(0)
+    _, eng, _ = _wet_engine(0, capillary="mlp")
+    eng.set_capnet(net)
+    ref.step(1)
+    eng.step(1)
+    a, b = ref.get_state(), eng.get_state()
+    scale = np.abs(a["force"]).max()
+    err = np.abs(a["force"] - b["force"]).max() / scale
+    assert err < 2e-2, err
+    s = eng.stats()
+    assert s["cap_mlp"] > 0
+    assert s["cap_fallback"] <= 0.2 * (s["cap_mlp"] + s["cap_fallback"])
+    # and over a run: the bed stays finite and close
+    ref.step(200)
+    eng.step(200)
+    eng.sync()
+    a, b = ref.get_state(), eng.get_state()
+    assert np.isfinite(b["pos"]).all()
+    assert np.abs(a["pos"] - b["pos"]).max() < 0.05 * w.setup.rad.max()
+    for e in (ref, eng):
+        e.close()
