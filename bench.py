@@ -152,6 +152,140 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def checksum(pos: np.ndarray) -> dict:
+    """FP64 sum of x + 2y + 3z, and a hash of the positions rounded to 1e-9 reduced units"""
+    p = np.asarray(pos, np.float64)
+    r = np.round(p * 1e9).astype(np.int64)
+    h = np.bitwise_xor.reduce((r[:, 0] * 73856093) ^ (r[:, 1] * 19349663) ^ (r[:, 2] * 83492791))
+    return {"sum": float((p[:, 0] + 2 * p[:, 1] + 3 * p[:, 2]).sum()), "hash": int(h)}
+
+
+def run_dry(args):
+    """The dry monodisperse gravity packing (5,000 spheres, 20,000 steps of
+    1e-6 s): this library's FP64 and mixed paths on the GPU and the oracle (the
+    reference's algorithm, FP64, all host cores) on the same start, each run
+    whole; packing fraction, coordination number and a positions checksum."""
+    import torch
+
+    from gpucode_gb300 import configs
+    from gpucode_gb300.engine import Engine, packing_metrics
+
+    w = configs.dry()
+    n, steps = w.setup.n, args.dry_steps
+    out = {}
+    for prec in ("mixed", "fp64"):
+        e = Engine(w.setup, precision=prec)
+        e.set_state(w.pos0_reduced)
+        e.step(16)
+        e.sync()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.step(steps - 16)
+        e.sync()
+        dt = time.perf_counter() - t0
+        pos = e.get_state()["pos"]
+        st = e.stats()
+        e.close()
+        m = packing_metrics(w.setup, pos)
+        out[prec] = {"particle_steps_per_s": n * (steps - 16) / dt, "wall_s": dt, "phi": m["phi"], "z": m["z"],
+                     "n_probe": m["n_probe"], "rebuilds": st["rebuilds"], "checksum": checksum(pos)}
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    if not pyoracle.ORACLE_LIB.exists():
+        pyoracle.build_oracle()
+    sim = pyoracle.OracleSim(w.setup, w.pos0_reduced)
+    t0 = time.perf_counter()
+    sim.step(steps)
+    dt = time.perf_counter() - t0
+    pos = sim.state()["pos"]
+    sim.close()
+    m = packing_metrics(w.setup, pos)
+    out["cpu_oracle"] = {"particle_steps_per_s": n * steps / dt, "wall_s": dt, "cores": threads, "phi": m["phi"],
+                         "z": m["z"], "n_probe": m["n_probe"], "checksum": checksum(pos)}
+    ref = out["cpu_oracle"]
+    for prec in ("mixed", "fp64"):
+        out[prec]["phi_rel_err_vs_oracle"] = abs(out[prec]["phi"] - ref["phi"]) / ref["phi"]
+        out[prec]["z_rel_err_vs_oracle"] = abs(out[prec]["z"] - ref["z"]) / ref["z"]
+    print(json.dumps({"metric": "particle-steps/s, 5k dry spheres, 20k steps; packing-frac & Z vs the oracle",
+                      "workload": "dry5k", "particles": n, "steps": steps, "dt_s": 1e-6, "data": "synthetic "
+                      "(seeded jittered hexagonal lattice)", "results": out}), flush=True)
+
+
+def run_ensemble(args):
+    """Batched ensemble: independent dry and wet packings of uneven sizes stepped
+    together by the same launches, block size / cell size / skin picked by the
+    autotuner on the batch; aggregate particle-steps/s, and each sampled
+    system's packing fraction against the same system run alone."""
+    import torch
+
+    from gpucode_gb300 import configs
+    from gpucode_gb300.autotune import autotune
+    from gpucode_gb300.engine import Engine, packing_metrics
+
+    t0 = time.perf_counter()
+    e = configs.ensemble(n_systems=args.ens_systems, steps=args.ens_steps)
+    t_build = time.perf_counter() - t0
+    comb = e.combined
+    systems = (e.system, e.cylinders, e.wet)
+    t0 = time.perf_counter()
+    setup, opts, tune = autotune(comb.inp, comb.dia, comb.pos0_reduced, None, skins=(0.5, 1.0, 2.0),
+                                 cells=(1.0, 1.3), blocks=(64, 128), warmup=10, trial=100, systems=systems)
+    t_tune = time.perf_counter() - t0
+    n = setup.n
+    eng = Engine(setup, precision="mixed", block_size=opts["block_size"])
+    eng.set_state(comb.pos0_reduced)
+    eng.set_systems(*systems)
+    eng.step(16)
+    eng.sync()
+    clk = Clocks()
+    clk.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.step(args.ens_steps - 16)
+    eng.sync()
+    dt = time.perf_counter() - t0
+    ck = clk.stop()
+    st = eng.stats()
+    pos = eng.get_state()["pos"]
+    eng.close()
+    rl = setup.s.unit.rlunit
+    picks = sorted(set(np.linspace(0, len(e.members) - 1, max(1, args.ens_alone)).astype(int).tolist()))
+    per_sys, alone_steps, alone_time = [], 0, 0.0
+    for k in picks:
+        m = configs.member_setup(e.members[k])
+        a = Engine(m.setup, precision="mixed")
+        a.set_state(m.pos0_reduced)
+        a.sync()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        a.step(args.ens_steps)
+        a.sync()
+        alone_time += time.perf_counter() - t1
+        alone_steps += m.setup.n * args.ens_steps
+        pa = a.get_state()["pos"]
+        a.close()
+        shift = np.array([e.offsets[k][0] / rl, e.offsets[k][1] / rl, 0.0])
+        mb = packing_metrics(m.setup, pos[e.system == k] - shift)
+        ma = packing_metrics(m.setup, pa)
+        per_sys.append({"system": k, "particles": m.setup.n, "wet": int(e.wet[k]), "phi_batched": mb["phi"],
+                        "phi_alone": ma["phi"], "phi_rel_diff": abs(mb["phi"] - ma["phi"]) / ma["phi"],
+                        "z_batched": mb["z"], "z_alone": ma["z"]})
+    diffs = [p["phi_rel_diff"] for p in per_sys]
+    print(json.dumps({
+        "metric": "aggregate particle-steps/s, batched ensemble of independent packings",
+        "workload": f"ensemble{args.ens_systems}", "value": n * (args.ens_steps - 16) / dt, "unit": UNIT,
+        "systems": args.ens_systems, "particles": n, "steps": args.ens_steps, "dt_s": 5e-7,
+        "data": "synthetic (seeded per-system deposits, log-normal sizes, counts uniform in [1000, 50000])",
+        "clocks": ck, "rebuilds": st["rebuilds"], "build_s": t_build, "autotune_s": t_tune, "autotune": tune,
+        "device_bytes": setup.memory()["total"],
+        "alone": {"systems_compared": len(per_sys), "particle_steps_per_s": alone_steps / max(alone_time, 1e-9),
+                  "phi_rel_diff_mean": float(np.mean(diffs)), "phi_rel_diff_max": float(np.max(diffs)),
+                  "per_system": per_sys}}), flush=True)
+
+
 def traffic_from_profiles() -> float | None:
     """DRAM bytes per launch of the fused step kernel from the committed ncu summary."""
     p = ROOT / "profiles" / "step_mixed_wet200k.md"
@@ -187,11 +321,26 @@ def main():
     ap.add_argument("--host-steps", action="store_true",
                     help="launch every step's kernels directly instead of from CUDA graphs (for ncu, which "
                          "cannot profile kernels of graphs with conditional nodes)")
+    ap.add_argument("--workload", default="wet200k", choices=["wet200k", "dry5k", "ensemble"],
+                    help="wet200k: the headline bench; dry5k: the dry lattice packing run whole on GPU and CPU; "
+                         "ensemble: independent packings batched in one engine")
+    ap.add_argument("--dry-steps", type=int, default=20000)
+    ap.add_argument("--ens-systems", type=int, default=256)
+    ap.add_argument("--ens-steps", type=int, default=10000)
+    ap.add_argument("--ens-alone", type=int, default=16, help="systems also run alone for the comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank = _dist()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.workload == "dry5k":
+        if rank == 0:
+            run_dry(args)
+        return
+    if args.workload == "ensemble":
+        if rank == 0:
+            run_ensemble(args)
         return
 
     import torch

@@ -131,6 +131,22 @@ class DemStats(C.Structure):
                 ("cap_fallback", C.c_longlong)]
 
 
+class DemMemory(C.Structure):
+    _fields_ = [("per_particle", C.c_longlong), ("per_slot", C.c_longlong), ("per_cell", C.c_longlong),
+                ("slots", C.c_longlong), ("total", C.c_longlong)]
+
+
+class DemTuneSpace(C.Structure):
+    _fields_ = [("n_skin", C.c_int), ("n_cell", C.c_int), ("n_block", C.c_int), ("pad", C.c_int),
+                ("skin_scale", C.c_double * 8), ("cell_scale", C.c_double * 8), ("block_size", C.c_int * 4),
+                ("warmup_steps", C.c_int), ("trial_steps", C.c_int)]
+
+
+class DemTuneResult(C.Structure):
+    _fields_ = [("skin_scale", C.c_double), ("cell_scale", C.c_double), ("block_size", C.c_int),
+                ("n_tried", C.c_int), ("best_rate", C.c_double), ("rate", C.c_double * 64)]
+
+
 class CapnetFitOpts(C.Structure):
     _fields_ = [("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_float), ("val_frac", C.c_float),
                 ("seed", C.c_ulonglong)]
@@ -212,6 +228,14 @@ def _declare(lib: C.CDLL) -> None:
         "dem_packing_metrics": (I, [I, P, P, P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(I)]),
         "dem_l2_flush": (I, [P, P, C.c_size_t]),
         "dem_compat_errors": (I, []),
+        "dem_set_systems": (I, [P, I, P, P, P]),
+        "dem_scale_cells": (I, [C.POINTER(DemSetup), C.c_double]),
+        "dem_autotune": (I, [C.POINTER(DemInput), P, P, P, C.POINTER(DemOptions), C.POINTER(DemTuneSpace), I, P, P, P,
+                             C.POINTER(DemSetup), C.POINTER(DemOptions), C.POINTER(DemTuneResult)]),
+        "dem_pack_deposit": (I, [I, P, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, I,
+                                 C.c_ulonglong, P]),
+        "dem_memory_estimate": (I, [C.POINTER(DemSetup), C.POINTER(DemOptions), C.POINTER(DemMemory)]),
+        "dem_fit_memory": (I, [C.POINTER(DemSetup), C.POINTER(DemOptions), C.c_double, I, C.POINTER(C.c_double)]),
         "dem_capnet_create": (I, [C.c_ulonglong, C.POINTER(P)]),
         "dem_capnet_destroy": (None, [P]),
         "dem_capnet_get": (I, [P, P, P]),

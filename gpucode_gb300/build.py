@@ -34,6 +34,7 @@ UNITS = [
     ("engine.cu", []),
     ("mixed.cu", []),
     ("capnet.cu", []),
+    ("tune.cu", []),
 ]
 
 

@@ -222,11 +222,7 @@ def hex_lattice(n: int, d: float, R: float, z0: float, spacing: float, jitter: f
 
 def deposit(dia: np.ndarray, R: float, z0: float, gap: float, tries: int, seed: int) -> np.ndarray:
     """Seeded sequential deposition (libdem_gb300's dem_pack_deposit)."""
-    lib = _abi.load()
-    f = lib.dem_pack_deposit
-    f.restype = C.c_int
-    f.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
-                  C.c_ulonglong, C.c_void_p]
+    f = _abi.load().dem_pack_deposit
     d = np.ascontiguousarray(dia, np.float64)
     out = np.zeros((len(d), 3), np.float64)
     _abi.check(f(len(d), _abi.ptr(d), 0.0, 0.0, R, z0, gap, tries, seed, _abi.ptr(out)), "dem_pack_deposit")
@@ -284,3 +280,91 @@ def small_dry(n: int = 600, seed: int = 3) -> Workload:
 def small_wet(n: int = 800, seed: int = 4, n_levels: int = 3) -> Workload:
     """Polydisperse wet bed of a few hundred spheres, for parity tests."""
     return wet(n=n, cyl_r=5e-3, seed=seed, steps=200, n_levels=n_levels)
+
+
+@dataclass
+class Ensemble:
+    """Independent packings laid out side by side in one domain (one set-up,
+    one engine), plus each packing's own set-up for running it alone."""
+
+    combined: Workload       # all systems: one set-up, concatenated particles
+    system: np.ndarray       # system of each particle of `combined` (caller order)
+    cylinders: list          # CylinderBC per system, reduced units of `combined`
+    wet: np.ndarray          # 1: capillary bridges act in that system
+    members: list            # Workload per system, its cylinder on the axis (0, 0)
+    offsets: np.ndarray      # SI (x, y) of each system's axis in the combined domain
+
+
+def ensemble(n_systems: int = 256, n_range: tuple = (1000, 50000), seed: int = 3, dt: float = 5e-7,
+             steps: int = 10000, n_levels: int = 4, skin_d: float = 1e-4, bridge_frac: float = 0.0125,
+             phi_fill: float = 0.6, gap: float = 6e-3, threads: int | None = None) -> Ensemble:
+    """n_systems packings, particle counts uniform in n_range (seeded), the wet
+    workload's diameter distribution per system, cylinder radius chosen so the
+    fill height is about three radii, every other system wet.  Systems are
+    deposited independently (in parallel host threads) and placed on shelves
+    with `gap` between cylinder walls, wider than any neighbour search, so no
+    pair ever spans two systems."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    rng = _rng(seed)
+    counts = rng.integers(n_range[0], n_range[1] + 1, n_systems)
+    wet = np.array([k % 2 for k in range(n_systems)], np.int32)
+    dias = [lognormal_diameters(int(n), 1e-3, 0.2, 0.5e-3, 2.0e-3, seed * 1000 + k) for k, n in enumerate(counts)]
+    radii = np.array([(np.sum(np.pi / 6 * d ** 3) / (phi_fill * 3 * np.pi)) ** (1 / 3) for d in dias])
+    _abi.load()  # bind the library once, before the worker threads use it
+    with ThreadPoolExecutor(threads) as ex:
+        pos = list(ex.map(lambda k: deposit(dias[k], float(radii[k]), 0.0, 0.0, 8, seed * 7919 + k),
+                          range(n_systems)))
+    real = 2.0e-3
+    rmin = min(float(d.min()) for d in dias) / 2
+    rmax = max(float(d.max()) for d in dias) / 2
+    cut_gap = (skin_d / real) * rmax / rmin
+    yldp = yldp_for_yield_overlap(0.01, E_YOUNG, NU)
+    dmpn = calibrate_dmpn(0.7, 0.5, 1e-3, RHO, E_YOUNG, NU, yldp)
+    liquid = (0.072, 6.0 * bridge_frac, 5e-6)
+    tops = np.array([float((p[:, 2] + d / 2).max()) + 10 * real for p, d in zip(pos, dias)])
+    # shelves, largest first, in a square of about the total footprint
+    order = np.argsort(-radii, kind="stable")
+    side = math.sqrt(float(np.sum((2 * radii + gap) ** 2))) * 1.05
+    centres = np.zeros((n_systems, 2))
+    x = y = 0.0
+    row_h = 0.0
+    width = 0.0
+    for k in order:
+        d = 2 * radii[k]
+        if x > 0 and x + d > side:
+            y += row_h + gap
+            x, row_h = 0.0, 0.0
+        centres[k] = (x + radii[k], y + radii[k])
+        x += d + gap
+        row_h = max(row_h, d)
+        width = max(width, x - gap)
+    height = y + row_h
+    half = 0.5 * max(width, height)
+    centres -= np.array([width / 2, height / 2])
+    dia_all = np.concatenate(dias)
+    pos_all = np.concatenate([p + np.array([c[0], c[1], 0.0]) for p, c in zip(pos, centres)])
+    system = np.concatenate([np.full(len(d), k, np.int32) for k, d in enumerate(dias)])
+    inp = make_input(len(dia_all), n_levels, real, cut_gap, half, float(tops.max()), RHO, E_YOUNG, NU, MU, dmpn,
+                     yldp, 1, liquid=liquid, dt=dt)
+    combined = Workload(f"ensemble{n_systems}", inp, dia_all, pos_all, Setup.build(inp, dia_all), steps)
+    rl = combined.setup.s.unit.rlunit
+    cylinders = []
+    for k in range(n_systems):
+        c = _abi.CylinderBC()
+        c.cir_x, c.cir_y = centres[k][0] / rl, centres[k][1] / rl
+        c.R, c.Tw, c.Bw, c.topv, c.btmv = radii[k] / rl, tops[k] / rl, 0.0, 0.0, 0.0
+        cylinders.append(c)
+    members = []
+    for k in range(n_systems):
+        mi = make_input(int(counts[k]), n_levels, real, cut_gap, float(radii[k]), float(tops[k]), RHO, E_YOUNG,
+                        NU, MU, dmpn, yldp, int(wet[k]), liquid=liquid if wet[k] else (0.0, 0.0, 0.0), dt=dt)
+        members.append(Workload(f"system{k}", mi, dias[k], pos[k], None, steps))
+    return Ensemble(combined, system, cylinders, wet, members, centres)
+
+
+def member_setup(m: Workload) -> Workload:
+    """the member's own set-up (built on demand: one per system alone)"""
+    if m.setup is None:
+        m.setup = Setup.build(m.inp, m.dia)
+    return m

@@ -264,12 +264,14 @@ __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* _
 /* CirWallListG (kernel.cu:1034-1073) */
 __global__ void k_wall_list(const double3* __restrict__ pos, const double* __restrict__ rad,
                             const CylinderBC* __restrict__ cyl, int* __restrict__ wlist, size_t pitch,
-                            int* __restrict__ nwall, int n, double search_gap) {
+                            int* __restrict__ nwall, int n, double search_gap, const int* __restrict__ id,
+                            const int* __restrict__ sys_of_id) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double3 p = pos[i];
   const double r = rad[i];
-  const CylinderBC c = *cyl;
+  /* batched systems: each particle meets its own system's cylinder */
+  const CylinderBC c = cyl[sys_of_id ? sys_of_id[id[i]] : 0];
   int* row = (int*)((char*)wlist + (size_t)i * pitch);
   int m = 0;
   if (p.z >= (c.Tw - (2.0 * r + search_gap))) row[m++] = 0;
@@ -410,9 +412,11 @@ dem_status neighbor_find(const double3* pos, const double* rad, const int* sorte
 }
 
 dem_status wall_list(const double3* pos, const double* rad, const CylinderBC* cyl, int* wlist, size_t pitch,
-                     int* nwall, int n, const DevConsts& k, cudaStream_t stream) {
+                     int* nwall, int n, const DevConsts& k, cudaStream_t stream, const int* id,
+                     const int* sys_of_id) {
   if (n <= 0) return DEM_OK;
-  k_wall_list<<<grid_for(n, 128), 128, 0, stream>>>(pos, rad, cyl, wlist, pitch, nwall, n, k.prm.SearchGap);
+  k_wall_list<<<grid_for(n, 128), 128, 0, stream>>>(pos, rad, cyl, wlist, pitch, nwall, n, k.prm.SearchGap, id,
+                                                    sys_of_id);
   return cuda_check(cudaGetLastError(), "wall_list launch");
 }
 

@@ -126,9 +126,11 @@ dem_status neighbor_find(const double3* pos, const double* rad, const int* sorte
                          int* num_nebor, int n, int* err, cudaStream_t stream,
                          Prefilter pre = Prefilter{nullptr, 0.f});
 
-/* CirWallListG (kernel.cu:1034-1073); wall list pitched rows */
+/* CirWallListG (kernel.cu:1034-1073); wall list pitched rows.  Batched
+ * systems: sys_of_id[id[i]] selects particle i's cylinder in cyl[] (NULL: cyl[0]). */
 dem_status wall_list(const double3* pos, const double* rad, const CylinderBC* cyl, int* wlist,
-                     size_t pitch, int* nwall, int n, const DevConsts& k, cudaStream_t stream);
+                     size_t pitch, int* nwall, int n, const DevConsts& k, cudaStream_t stream,
+                     const int* id = nullptr, const int* sys_of_id = nullptr);
 
 /* HstryCopyG (kernel.cu:869-911).  For re-ordered particles: old_src maps a
  * particle's new index to its previous index (NULL: unchanged), nebor_idx_old

@@ -280,7 +280,7 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
   st = neighbor_find(b.pos, b.rad, reorder ? nullptr : b.sorted_src, b.cell_start, b.cell_end, b.plevel, b.nidx,
                      c->lv, c->k, b.nebor, b.num_nebor, n, b.err, s, pre);
   if (st != DEM_OK) return st;
-  st = wall_list(b.pos, b.rad, b.cyl, b.wlist, 3 * sizeof(int), b.nwall, n, c->k, s);
+  st = wall_list(b.pos, b.rad, b.cyl, b.wlist, 3 * sizeof(int), b.nwall, n, c->k, s, b.id, b.sys_of_id);
   if (st != DEM_OK) return st;
   k_carry<<<grid_for(n, 128), 128, 0, s>>>(b.nebor, b.num_nebor, b.nidx, b.plevel, b.npars, b.nneb, b.nebor_old,
                                            b.num_nebor_old, b.nidx_old, b.rec_old, b.brg_old, b.rec, b.brg, b.wlist,
@@ -416,6 +416,84 @@ int graph_len(const dem_ctx* c) { return c->opt.graph_steps > 0 ? c->opt.graph_s
 
 using namespace dem;
 
+namespace {
+
+/* device bytes of dem_create for N particles, S slots, C cells: the sums of
+ * its allocation list (kept next to it), plus 2 MiB of rounding per allocation */
+dem_memory memory_of(long long N, long long S, long long C, const dem_options* o) {
+  dem_memory m;
+  m.per_particle = 3 * 24 + 2 * 8 + 5 * 4      /* pos vel angv, rad pmove, lqd lqd_old id plevel nidx */
+                   + 3 * 24 + 8 + 3 * 4        /* tmp copies used while permuting */
+                   + 2 * 24 + 8                /* force mom rmom */
+                   + 4 + 12 + 4 + 4 + 12 + 4 + 4 /* num_nebor wlist nwall and their copies, nidx_old */
+                   + 2 * 3 * 64                /* wall records and their copies */
+                   + 3 * 4 + 2 * 4;            /* sorted hash / source, old_to_new, sort scratch */
+  if (o && o->precision == DEM_PREC_MIXED) m.per_particle += 9 * 16; /* FP32 shadows */
+  m.per_slot = 2 * (4 + 64 + 1);               /* list entry, record, bridge flag, and their copies */
+  m.per_cell = 2 * 4;
+  m.slots = S;
+  const long long allocations = 64;
+  m.total = N * m.per_particle + S * m.per_slot + C * m.per_cell + ((C + 2047) / 2048 + 64) * 4 +
+            allocations * (2LL << 20);
+  if (o && o->capillary == DEM_CAP_MLP) m.total += 16 << 10;
+  return m;
+}
+
+}  // namespace
+
+extern "C" dem_status dem_memory_estimate(const dem_setup* s, const dem_options* o, dem_memory* out) {
+  if (!s || !out) return fail(DEM_ERR_ARG, "dem_memory_estimate: null argument");
+  dem_options d;
+  if (!o) {
+    dem_default_options(&d);
+    o = &d;
+  }
+  *out = memory_of(s->np, s->n_pp_slots, s->sys_ncells, o);
+  return DEM_OK;
+}
+
+extern "C" dem_status dem_fit_memory(dem_setup* s, const dem_options* o, double budget_bytes, int min_slots,
+                                     double* factor) {
+  if (!s || min_slots < 1 || !(budget_bytes > 0.0)) return fail(DEM_ERR_ARG, "dem_fit_memory: bad arguments");
+  dem_options d;
+  if (!o) {
+    dem_default_options(&d);
+    o = &d;
+  }
+  const int L = s->n_levels;
+  auto slots_at = [&](double f, int* nneb) {
+    long long S = 0;
+    for (int l = 0; l < L; l++) {
+      const int orig = s->level_nnebors[l];
+      int v = (int)std::floor(f * orig);
+      v = std::min(orig, std::max(v, std::min(min_slots, orig)));
+      if (nneb) nneb[l] = v;
+      S += (long long)v * s->level_npars[l];
+    }
+    return S;
+  };
+  auto bytes_at = [&](double f) { return (double)memory_of(s->np, slots_at(f, nullptr), s->sys_ncells, o).total; };
+  double f = 1.0;
+  if (bytes_at(1.0) > budget_bytes) {
+    if (bytes_at(0.0) > budget_bytes)
+      return fail(DEM_ERR_NOMEM, "dem_fit_memory: " + std::to_string(s->np) + " particles do not fit " +
+                                     std::to_string(budget_bytes / 1e9) + " GB even at " +
+                                     std::to_string(min_slots) + " slots per particle");
+    double lo = 0.0, hi = 1.0;
+    for (int it = 0; it < 60; it++) {
+      const double mid = 0.5 * (lo + hi);
+      if (bytes_at(mid) <= budget_bytes) lo = mid;
+      else hi = mid;
+    }
+    f = lo;
+  }
+  int nneb[DEM_MAX_LEVELS];
+  s->n_pp_slots = slots_at(f, nneb);
+  for (int l = 0; l < L; l++) s->level_nnebors[l] = nneb[l];
+  if (factor) *factor = f;
+  return DEM_OK;
+}
+
 extern "C" void dem_default_options(dem_options* o) {
   std::memset(o, 0, sizeof(*o));
   o->precision = DEM_PREC_MIXED;
@@ -534,6 +612,46 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   }
   *out = c;
   return DEM_OK;
+}
+
+extern "C" dem_status dem_set_systems(dem_ctx* c, int n_sys, const int* system_of_particle, const CylinderBC* cyl,
+                                      const int* wet) {
+  if (!c || n_sys < 1 || !system_of_particle || !cyl) return fail(DEM_ERR_ARG, "dem_set_systems: bad arguments");
+  if (c->opt.precision != DEM_PREC_MIXED)
+    return fail(DEM_ERR_ARG, "dem_set_systems: batched systems run on the mixed-precision path");
+  if (c->b.sys_of_id) return fail(DEM_ERR_STATE, "dem_set_systems: the systems are already set");
+  for (int i = 0; i < c->n; i++)
+    if (system_of_particle[i] < 0 || system_of_particle[i] >= n_sys)
+      return fail(DEM_ERR_ARG, "dem_set_systems: particle " + std::to_string(i) + " has system " +
+                                   std::to_string(system_of_particle[i]) + " outside [0, " +
+                                   std::to_string(n_sys) + ")");
+  std::vector<int> w(n_sys, c->s.force_cap == 1 ? 1 : 0);
+  if (wet)
+    for (int k = 0; k < n_sys; k++) w[k] = wet[k] ? 1 : 0;
+  EngineBufs& b = c->b;
+  CylinderBC* cyls = nullptr;
+  int *sys = nullptr, *sw = nullptr;
+  dem_status st = dalloc(c, &cyls, (size_t)n_sys);
+  if (st == DEM_OK) st = dalloc(c, &sys, (size_t)c->n);
+  if (st == DEM_OK) st = dalloc(c, &sw, (size_t)n_sys);
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (st != DEM_OK) return;
+    cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) st = cuda_check(e, "dem_set_systems upload");
+  };
+  up(cyls, cyl, sizeof(CylinderBC) * (size_t)n_sys);
+  up(sys, system_of_particle, sizeof(int) * (size_t)c->n);
+  up(sw, w.data(), sizeof(int) * (size_t)n_sys);
+  if (st != DEM_OK) return st;
+  b.cyl = cyls;
+  b.sys_of_id = sys;
+  b.sys_wet = sw;
+  b.n_sys = n_sys;
+  /* graphs captured the single-cylinder pointers: rebuild them; and the wall
+   * lists must be rebuilt against the new cylinders */
+  destroy_graph(c);
+  const int one = 1;
+  return cuda_check(cudaMemcpy(b.need, &one, sizeof(int), cudaMemcpyHostToDevice), "dem_set_systems");
 }
 
 extern "C" dem_status dem_destroy(dem_ctx* c) {
@@ -867,6 +985,7 @@ const char kMagic[8] = {'D', 'E', 'M', 'G', 'B', '3', '0', '1'};
 extern "C" dem_status dem_save(dem_ctx* c, const char* path, int nBatch) {
   if (!c || !path) return fail(DEM_ERR_ARG, "dem_save: null argument");
   dem_status st = DEM_OK;
+  if (c->b.sys_of_id) return fail(DEM_ERR_STATE, "dem_save: checkpoints of batched systems are not supported");
   if (c->opt.precision == DEM_PREC_MIXED && c->parity != 0)
     return fail(DEM_ERR_STATE, "dem_save: call after an even number of steps");
   cudaError_t e = cudaStreamSynchronize(c->stream);

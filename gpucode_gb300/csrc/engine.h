@@ -53,7 +53,11 @@ struct EngineBufs {
   int3* grid_size;
   int *ncell_idx, *npars, *nneb;
   double* level_size;
-  CylinderBC* cyl;
+  CylinderBC* cyl; /* one cylinder, or one per system when systems are batched */
+  /* batched systems (NULL for one system): system of each particle id, and
+   * whether each system is wet */
+  int *sys_of_id, *sys_wet;
+  int n_sys;
   /* control words: flag (rebuild count from the integrator), need (host
    * request), err (error bits), counters (u64[8]) */
   int *flag, *need, *err;

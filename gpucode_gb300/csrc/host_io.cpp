@@ -641,6 +641,29 @@ extern "C" int ParticleFeed(FeedZone* Feedcube, CylinderBC* h_Cir, double InitPa
 /* seeded deposition packer (benchmark and test inputs)                     */
 /* ---------------------------------------------------------------------- */
 
+extern "C" dem_status dem_scale_cells(dem_setup* s, double factor) {
+  if (!s || !(factor >= 1.0) || factor > 16.0) return dem::fail(DEM_ERR_ARG, "dem_scale_cells: factor must be in [1, 16]");
+  if (factor == 1.0) return DEM_OK;
+  /* larger cells keep every pair within one cell of each other, so the
+   * neighbour search (the 27 surrounding cells of each level) stays complete */
+  dem_setup t = *s;
+  long long total = 0;
+  for (int i = 0; i < t.n_levels; i++) {
+    t.cell_size[i] *= factor;
+    t.grid_size[i].x = (int)std::ceil((t.prm.EndPoint.x - t.prm.Origin.x) / t.cell_size[i]);
+    t.grid_size[i].y = (int)std::ceil((t.prm.EndPoint.y - t.prm.Origin.y) / t.cell_size[i]);
+    t.grid_size[i].z = (int)std::ceil((t.prm.EndPoint.z - t.prm.Origin.z) / t.cell_size[i]);
+    const long long nc = (long long)t.grid_size[i].x * t.grid_size[i].y * t.grid_size[i].z;
+    if (nc <= 0) return dem::fail(DEM_ERR_ARG, "dem_scale_cells: empty grid");
+    t.num_cells[i] = (int)nc;
+    total += nc;
+    t.ncell_idx[i] = (int)total;
+  }
+  t.sys_ncells = (int)total;
+  *s = t;
+  return DEM_OK;
+}
+
 extern "C" dem_status dem_pack_deposit(int n, const double* dia, double cx, double cy, double R, double z0,
                                        double gap, int tries, unsigned long long seed, double3* pos_out) {
   if (n <= 0 || !dia || !pos_out || R <= 0.0 || tries < 1)

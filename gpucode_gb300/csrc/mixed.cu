@@ -89,6 +89,9 @@ struct MixArgs {
   float dtf, coarse_tol, rfrc;
   float lqd_vol, lqd_layer, lqd_gapmn, lqd_st;
   Law32 pp, pw;
+  /* batched systems (NULL for one system): system of each particle id (its
+   * cylinder is cyl[system]) and whether the system is wet */
+  const int *sys_of_id, *sys_wet;
   /* learned capillary closure (NET variant only) */
   const int* id;
   const CapNetSmem* capw;
@@ -405,6 +408,9 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
   F.z.add(-mass_f); /* gravity, m = (2r)^3 */
   int wet = 0;
   float iVol = 0.f;
+  /* batched systems: this particle's system (its cylinder, dry or wet) */
+  const int sys = a.sys_of_id ? a.sys_of_id[ro(a.id + qq)] : 0;
+  const bool wet_i = WET && (!a.sys_wet || a.sys_wet[sys]);
   if (WET) {
     int inl = __float_as_int(vi4.w);
     if (inl < 12) inl = 12;
@@ -486,7 +492,7 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
         ncont++;
       }
     }
-    if (WET) {
+    if (WET && wet_i) {
       int jnl = __float_as_int(vj4.w);
       if (jnl < 12) jnl = 12;
       const float tj = 2.0f * rj;
@@ -557,7 +563,7 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
   const int nw = live ? a.nwall[qq] : 0;
   if (nw > 0) {
     const double rid = a.rad[qq];
-    const CylinderBC cy = *a.cyl;
+    const CylinderBC cy = a.cyl[sys];
     double3 jvel = make_double3(0.0, 0.0, 0.0);
     for (int w = 0; w < nw; w++) {
       const int kind = a.wlist[3 * qq + w];
@@ -782,6 +788,7 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   a.nebor = b.nebor; a.num_nebor = b.num_nebor; a.plevel = b.plevel; a.nidx = b.nidx; a.npars = b.npars;
   a.nneb = b.nneb; a.rec = b.rec; a.brg = b.brg; a.wlist = b.wlist; a.nwall = b.nwall; a.wrec = b.wrec;
   a.force_out = m->force; a.flag = b.flag; a.err = b.err; a.counters = b.counters; a.cyl = b.cyl;
+  a.sys_of_id = b.sys_of_id; a.sys_wet = b.sys_wet;
   a.n = c->n;
   a.force_cap = c->s.force_cap;
   a.off = m->off;
@@ -804,7 +811,9 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   a.capw = reinterpret_cast<const CapNetSmem*>(c->cap_w);
   a.theta_seed = c->theta_seed;
   a.theta_max = c->theta_max;
-  const int bs = 32 * kWarps;
+  /* threads per block: the option (a multiple of 32 up to 128), else 128 */
+  const int ob = c->opt.block_size;
+  const int bs = (ob >= 32 && ob <= 32 * kWarps && ob % 32 == 0) ? ob : 32 * kWarps;
   if (c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP) {
     if (!c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
     k_step_mixed<true, true><<<grid_for(c->n, bs), bs, kCapSmem, s>>>(a);

@@ -58,6 +58,41 @@ class Setup:
         """SI lengths -> reduced lengths (divide by REALSIZE, UnitReduce.cpp:14)."""
         return np.asarray(x_m, np.float64) / self.s.unit.rlunit
 
+    def memory(self, precision: str = "mixed", capillary: str = "formula") -> dict:
+        """device bytes the engine allocates for this set-up (dem_memory_estimate)"""
+        lib = _abi.load()
+        m = _abi.DemMemory()
+        check(lib.dem_memory_estimate(C.byref(self.s), C.byref(_options(precision, capillary)), C.byref(m)),
+              "dem_memory_estimate")
+        return {k: getattr(m, k) for k, _ in _abi.DemMemory._fields_}
+
+    def scale_cells(self, factor: float) -> None:
+        """multiply every level's cell size by factor >= 1 (dem_scale_cells)"""
+        check(_abi.load().dem_scale_cells(C.byref(self.s), float(factor)), "dem_scale_cells")
+
+    def fit_memory(self, budget_bytes: float, min_slots: int = 8, precision: str = "mixed",
+                   capillary: str = "formula") -> float:
+        """scale the neighbour slots so the engine fits budget_bytes (dem_fit_memory); returns the factor"""
+        lib = _abi.load()
+        f = C.c_double()
+        check(lib.dem_fit_memory(C.byref(self.s), C.byref(_options(precision, capillary)), float(budget_bytes),
+                                 int(min_slots), C.byref(f)), "dem_fit_memory")
+        return f.value
+
+
+def _options(precision: str = "mixed", capillary: str = "formula", reorder: bool = True, use_graph: bool = True,
+             graph_steps: int = 0, block_size: int = 0) -> DemOptions:
+    lib = _abi.load()
+    opt = DemOptions()
+    lib.dem_default_options(C.byref(opt))
+    opt.precision = {"mixed": _abi.PREC_MIXED, "fp64": _abi.PREC_FP64}[precision]
+    opt.capillary = {"formula": _abi.CAP_FORMULA, "mlp": _abi.CAP_MLP}[capillary]
+    opt.reorder = 1 if reorder else 0
+    opt.use_graph = 1 if use_graph else 0
+    opt.graph_steps = int(graph_steps)
+    opt.block_size = int(block_size)
+    return opt
+
 
 def packing_metrics(setup: Setup, pos: np.ndarray) -> dict:
     """Packing fraction and mean coordination number of a bed (dem_packing_metrics)."""
@@ -75,16 +110,10 @@ class Engine:
     """One simulation on one GPU (dem_ctx)."""
 
     def __init__(self, setup: Setup, precision: str = "mixed", reorder: bool = True, use_graph: bool = True,
-                 capillary: str = "formula", graph_steps: int = 0):
+                 capillary: str = "formula", graph_steps: int = 0, block_size: int = 0):
         self.lib = _abi.load()
         self.setup = setup
-        opt = DemOptions()
-        self.lib.dem_default_options(C.byref(opt))
-        opt.precision = {"mixed": _abi.PREC_MIXED, "fp64": _abi.PREC_FP64}[precision]
-        opt.capillary = {"formula": _abi.CAP_FORMULA, "mlp": _abi.CAP_MLP}[capillary]
-        opt.reorder = 1 if reorder else 0
-        opt.use_graph = 1 if use_graph else 0
-        opt.graph_steps = int(graph_steps)
+        opt = _options(precision, capillary, reorder, use_graph, graph_steps, block_size)
         self.opt = opt
         h = C.c_void_p()
         check(self.lib.dem_create(C.byref(setup.s), ptr(setup.rad), ptr(setup.plevel), ptr(setup.nidx),
@@ -139,6 +168,16 @@ class Engine:
 
     def set_contact_angles(self, theta_max_rad: float, seed: int = 0) -> None:
         check(self.lib.dem_set_contact_angles(self.h, float(theta_max_rad), int(seed)), "dem_set_contact_angles")
+
+    # ---- batched systems ----
+    def set_systems(self, system_of_particle: np.ndarray, cylinders: list, wet: np.ndarray | None = None) -> None:
+        """independent packings stepped together (dem_set_systems); cylinders are
+        CylinderBC structs in reduced units, one per system"""
+        sysv = np.ascontiguousarray(system_of_particle, np.int32).reshape(self.n)
+        arr = (_abi.CylinderBC * len(cylinders))(*cylinders)
+        w = None if wet is None else np.ascontiguousarray(wet, np.int32).reshape(len(cylinders))
+        check(self.lib.dem_set_systems(self.h, len(cylinders), ptr(sysv), C.cast(arr, C.c_void_p),
+                                       None if w is None else ptr(w)), "dem_set_systems")
 
     def save(self, path: str | os.PathLike, nbatch: int = 1) -> None:
         check(self.lib.dem_save(self.h, str(path).encode(), nbatch), "dem_save")

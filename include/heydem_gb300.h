@@ -330,6 +330,15 @@ dem_status dem_get_history(dem_ctx* c, double* rec, int* brg, int max_per);
  * wrec[np][3][8] (as dem_get_history), and the pending rebuild flag.  Any
  * pointer may be NULL. */
 dem_status dem_get_aux(dem_ctx* c, double* pmove, int* lqd, int* nwall, int* wlist, double* wrec, int* flag);
+/* Batched systems (no counterpart in the reference): the context's particles
+ * belong to n_sys independent packings laid out side by side in its domain
+ * (no two systems within a neighbour search distance of each other), stepped
+ * together by the same launches.  system_of_particle[np] (caller order) gives
+ * each particle's system, cyl[n_sys] (reduced units) each system's container
+ * and wet[n_sys] (NULL: the set-up's force_cap for all) whether its bridges
+ * act.  Mixed precision only; call once, before stepping the systems. */
+dem_status dem_set_systems(dem_ctx* c, int n_sys, const int* system_of_particle, const CylinderBC* cyl,
+                           const int* wet);
 /* Write / read the full engine state (binary, with the reference's
  * "SYSTEM Info" text header so LoadPara can parse it). */
 dem_status dem_save(dem_ctx* c, const char* path, int nBatch);
@@ -378,6 +387,51 @@ dem_status dem_pack_deposit(int n, const double* dia, double cx, double cy, doub
  * p-p contacts of the spheres centred in the probe. */
 dem_status dem_packing_metrics(int n, const double3* pos, const double* rad, const CylinderBC* cyl, double* phi,
                                double* z_mean, int* n_probe);
+/* ---- memory plan (no counterpart in the reference) ----
+ * Device bytes dem_create allocates for a set-up and options. */
+typedef struct dem_memory {
+  long long per_particle;  /* bytes per particle (state, copies, wall lists and records, sort) */
+  long long per_slot;      /* bytes per neighbour slot (list, record, bridge flag, and their copies) */
+  long long per_cell;      /* bytes per cell (ranges, scan tiles) */
+  long long slots;         /* neighbour slots of the set-up */
+  long long total;         /* all of it, plus small fixed tables */
+} dem_memory;
+dem_status dem_memory_estimate(const dem_setup* s, const dem_options* o, dem_memory* out);
+/* Scale every level's neighbour slots by one factor f <= 1 (each level keeps
+ * at least min_slots) so that dem_create's allocation fits budget_bytes;
+ * updates s->level_nnebors and s->n_pp_slots and returns f.  The reference's
+ * slot formula (ReadData.cpp:302) reserves ~100 slots per particle where a
+ * packed bed uses a few; a level that outgrows its slots is reported by
+ * dem_sync as DEM_ERR_OVERFLOW, never written past.  DEM_ERR_NOMEM if even
+ * min_slots does not fit. */
+dem_status dem_fit_memory(dem_setup* s, const dem_options* o, double budget_bytes, int min_slots, double* factor);
+
+/* ---- cell size and the autotuner (no counterpart in the reference) ----
+ * Multiply every level's cell size by factor in [1, 16] and rederive the
+ * grids (larger cells keep the 27-cell neighbour search complete). */
+dem_status dem_scale_cells(dem_setup* s, double factor);
+typedef struct dem_tune_space {
+  int n_skin, n_cell, n_block, pad;
+  double skin_scale[8];   /* multiples of the input's CUTGAPFORNEIGHBORLIST */
+  double cell_scale[8];   /* factors for dem_scale_cells */
+  int block_size[4];      /* threads per block of the step kernel (multiples of 32, <= 128) */
+  int warmup_steps;       /* untimed steps of each trial (the first builds the lists) */
+  int trial_steps;        /* timed steps of each trial */
+} dem_tune_space;
+typedef struct dem_tune_result {
+  double skin_scale, cell_scale;
+  int block_size, n_tried;
+  double best_rate;       /* particle-steps/s of the chosen candidate */
+  double rate[64];        /* every candidate, skin-major then cell then block */
+} dem_tune_result;
+/* Time every candidate of `space` on the given bed (positions / velocities in
+ * the set-up's reduced units; batched systems as dem_set_systems, n_sys = 0
+ * for one system) and return the fastest one's set-up and options. */
+dem_status dem_autotune(const dem_input* in, const double* dia, const double3* pos, const double3* vel,
+                        const dem_options* base, const dem_tune_space* space, int n_sys,
+                        const int* system_of_particle, const CylinderBC* cyl, const int* wet,
+                        dem_setup* best_setup, dem_options* best_opt, dem_tune_result* rep);
+
 /* ---- learned capillary closure (no counterpart in the reference) ----
  * A 4 -> 64 -> 64 -> 2 SiLU network standing in for the reference's capillary
  * routine fCap (kernel.cu:65-81) and rupture distance (kernel.cu:518).
