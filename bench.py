@@ -286,9 +286,244 @@ def run_ensemble(args):
                   "per_system": per_sys}}), flush=True)
 
 
-def traffic_from_profiles() -> float | None:
+def train_closure(samples: int, epochs: int, settle: int = 2000, snaps: int = 11):
+    """The learned capillary closure as the wet workloads deploy it: samples of
+    the plain formula logged from the 200,000-sphere wet bed while it settles
+    (`snaps` points spread over `settle` steps), then trained on the GPU by the
+    library's own kernels (seeded 90/10 split, Adam lr 1e-3, batch 8192).
+    Returns (network, fit report, samples used)."""
+    import torch
+
+    from gpucode_gb300 import capnet as cn
+    from gpucode_gb300 import configs
+    from gpucode_gb300.engine import Engine
+
+    w = configs.wet()
+    e = Engine(w.setup, precision="mixed")
+    e.set_state(w.pos0_reduced)
+    per = -(-samples // snaps)
+    xs, ys = [], []
+    e.step(settle - snaps * (settle // (snaps + 1)))
+    for _ in range(snaps):
+        e.step(settle // (snaps + 1))
+        x, y = cn.collect_samples(e, per)
+        xs.append(x.clone())
+        ys.append(y.clone())
+    e.close()
+    x, y = torch.cat(xs).contiguous(), torch.cat(ys).contiguous()
+    net = cn.CapNet(seed=0)
+    rep = net.fit(x, y, epochs=epochs, batch=8192, lr=1e-3, val_frac=0.1, seed=2024)
+    return net, rep, int(len(x))
+
+
+def run_span(e, steps: int) -> tuple[float, dict]:
+    """`steps` graph-replayed steps of engine e, timed on the host around a
+    synchronised span (rebuilds included); -> (wall s, clocks)"""
+    import torch
+
+    e.sync()
+    clk = Clocks()
+    clk.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e.step(steps)
+    e.sync()
+    dt = time.perf_counter() - t0
+    return dt, clk.stop()
+
+
+def closure_error(e, net, capacity: int = 8_000_000) -> dict:
+    """per-contact error of the network against the plain formula (FP64, as
+    the reference evaluates it) over every bridge of engine e's current bed"""
+    import torch
+
+    from gpucode_gb300 import capnet as cn
+
+    x, _ = cn.collect_samples(e, capacity)
+    if len(x) == 0:
+        return {"bridges": 0}
+    # the step kernel evaluates the network only inside its training box (the
+    # formula takes the rest): the error is the network's over those bridges
+    _, norm = net.get()
+    lo = torch.tensor(norm[12:16], device=x.device)
+    hi = torch.tensor(norm[16:20], device=x.device)
+    inside = ((x >= lo) & (x <= hi)).all(dim=1)
+    n_all = len(x)
+    x = x[inside].contiguous()
+    if len(x) == 0:
+        return {"bridges": n_all, "outside_training_box": n_all}
+    yn = net.infer(x, True).double()
+    yf = cn.formula(x, True).double()
+    fe = (yn[:, 0] - yf[:, 0]).abs() / yf[:, 0].abs().clamp_min(1e-30)
+    re = (yn[:, 1] - yf[:, 1]).abs() / yf[:, 1].abs().clamp_min(1e-30)
+    q = torch.tensor([0.5, 0.99, 0.999], dtype=torch.float64, device=fe.device)
+    fq = torch.quantile(fe[: 10_000_000], q).tolist()
+    return {"bridges": n_all, "outside_training_box": n_all - int(len(x)),
+            "force_rel_err_mean": float(fe.mean()), "force_rel_err_p50": fq[0],
+            "force_rel_err_p99": fq[1], "force_rel_err_p999": fq[2], "force_rel_err_max": float(fe.max()),
+            "rupture_rel_err_mean": float(re.mean()), "rupture_rel_err_max": float(re.max())}
+
+
+def run_wet_full(args):
+    """The 200,000-sphere wet packing run whole (50,000 steps of 5e-7 s) three
+    ways from the same deposited bed: FP32 forces / FP64 state with the plain
+    capillary formula, the same with the learned closure fused in the step
+    kernel, and the all-FP64 engine (the reference's formulas).  Packing
+    fraction and coordination number at checkpoints along the run; the error
+    of each fast path against the FP64 run at the end."""
+    from gpucode_gb300 import configs
+    from gpucode_gb300.engine import Engine, packing_metrics
+
+    w = configs.wet()
+    n, total = w.setup.n, args.full_steps
+    every = max(1, total // 5)
+    net, rep, used = train_closure(args.capnet_samples, args.capnet_epochs)
+    runs = {}
+    for name, prec, cap in (("mixed_formula", "mixed", "formula"), ("mixed_mlp", "mixed", "mlp"),
+                            ("fp64", "fp64", "formula")):
+        e = Engine(w.setup, precision=prec, capillary=cap)
+        if cap == "mlp":
+            e.set_capnet(net)
+        e.set_state(w.pos0_reduced)
+        done, wall, marks, clocks = 0, 0.0, [], []
+        while done < total:
+            k = min(every, total - done)
+            dt, ck = run_span(e, k)
+            wall += dt
+            done += k
+            clocks.append(ck)
+            m = packing_metrics(w.setup, e.get_state()["pos"])
+            marks.append({"step": done, "phi": m["phi"], "z": m["z"], "n_probe": m["n_probe"]})
+        st = e.stats()
+        runs[name] = {"particle_steps_per_s": n * total / wall, "wall_s": wall, "rebuilds": st["rebuilds"],
+                      "checkpoints": marks, "clocks": clocks[-1]}
+        if cap == "mlp":
+            runs[name]["network_evaluations"] = st["cap_mlp"]
+            runs[name]["formula_fallbacks"] = st["cap_fallback"]
+            runs[name]["closure_error_final_bed"] = closure_error(e, net)
+        e.close()
+    net.close()
+    ref = runs["fp64"]["checkpoints"][-1]
+    for name in ("mixed_formula", "mixed_mlp"):
+        fin = runs[name]["checkpoints"][-1]
+        runs[name]["phi_rel_err_vs_fp64"] = abs(fin["phi"] - ref["phi"]) / ref["phi"]
+        runs[name]["z_rel_err_vs_fp64"] = abs(fin["z"] - ref["z"]) / max(ref["z"], 1e-300)
+        runs[name]["speedup_vs_fp64"] = runs[name]["particle_steps_per_s"] / runs["fp64"]["particle_steps_per_s"]
+    print(json.dumps({
+        "metric": METRIC, "workload": "wet200k-full", "unit": UNIT, "particles": n, "steps": total, "dt_s": 5e-7,
+        "data": "synthetic (seeded deposited bed, log-normal sizes)",
+        "timing": "host wall time around graph-replayed spans of steps, rebuilds included, metrics outside",
+        "closure_training": {"samples": used, "epochs": rep["epochs"], "fit_seconds": rep["seconds"],
+                             "val_force_rel_err_mean": rep["val_force_rel_mean"],
+                             "val_force_rel_err_max": rep["val_force_rel_max"]},
+        "targets": {"phi_rel_err": 0.002, "z_rel_err": 0.01}, "runs": runs}), flush=True)
+
+
+def run_wet_large(args, which: str):
+    """wet2m: 2,000,000 wet spheres in a 60 mm cylinder, 10,000 steps, the
+    learned closure (trained on the 200,000-sphere bed's samples) fused in the
+    step kernel with the plain formula outside its training box; per-contact
+    error of the network against the formula on the final bed, and the same
+    bed with the FP32 formula for comparison.
+    wet16m: 16,000,000 wet spheres in a 150 mm cylinder, 5,000 steps, slots
+    fitted to 180 GB, fused closure; the step kernel's HBM roofline on it; and
+    packing fraction / coordination number of a 1,000,000-sphere sub-cylinder
+    of the same set-up (37.5 mm: the same fill height) with the fused closure
+    against its all-FP64 plain run."""
+    import ctypes as C
+
+    import torch
+
+    from gpucode_gb300 import configs
+    from gpucode_gb300._abi import check
+    from gpucode_gb300.engine import Engine, packing_metrics
+
+    net, rep, used = train_closure(args.capnet_samples, args.capnet_epochs)
+    if which == "wet2m":
+        n_big, r_big, steps = 2_000_000, 60e-3, args.large_steps or 10000
+    else:
+        n_big, r_big, steps = 16_000_000, 150e-3, args.large_steps or 5000
+    t0 = time.perf_counter()
+    w = configs.wet(n=n_big, cyl_r=r_big, steps=steps)
+    t_gen = time.perf_counter() - t0
+    fit = None
+    if which == "wet16m":
+        budget = 180e9
+        full = w.setup.memory("mixed", "mlp")["total"]
+        fit = {"budget_bytes": budget, "unfitted_bytes": full, "slot_factor": 1.0}
+        if full > budget:
+            fit["slot_factor"] = w.setup.fit_memory(budget, min_slots=8, precision="mixed", capillary="mlp")
+        fit["device_bytes"] = w.setup.memory("mixed", "mlp")["total"]
+        fit["slots_per_level"] = list(w.setup.s.level_nnebors)[: w.setup.s.n_levels]
+    n = w.setup.n
+    out = {}
+    for name, cap in (("mixed_mlp", "mlp"), ("mixed_formula", "formula")):
+        e = Engine(w.setup, precision="mixed", capillary=cap)
+        if cap == "mlp":
+            e.set_capnet(net)
+        e.set_state(w.pos0_reduced)
+        e.step(16)
+        s0 = e.stats()
+        dt, ck = run_span(e, steps - 16)
+        s1 = e.stats()
+        ps = n * (steps - 16)
+        cnt = {k: (s1[k] - s0[k]) / ps for k in ("nb_entries", "contacts", "bridges", "wall_contacts")}
+        bpp = 152 + 4 * cnt["nb_entries"] + 128 * cnt["contacts"] + 16 * cnt["bridges"] + 128 * cnt["wall_contacts"]
+        ms_k = C.c_double()
+        check(e.lib.dem_profile_step(e.h, 5, None, 0, C.byref(ms_k)), "dem_profile_step")
+        peak, peak_kind = _peaks()
+        ach = n * bpp / (ms_k.value * 1e-3) / 1e9
+        m = packing_metrics(w.setup, e.get_state()["pos"])
+        r = {"particle_steps_per_s": ps / dt, "wall_s": dt, "rebuilds": s1["rebuilds"] - s0["rebuilds"],
+             "clocks": ck, "per_step_counts": cnt, "phi": m["phi"], "z": m["z"], "n_probe": m["n_probe"],
+             "roofline": {"kernel": step_kernel("auto", cap), "kernel_ms": ms_k.value, "bytes_per_particle": bpp,
+                          "achieved": ach, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                          "frac": ach / peak, "l2": "working set far above L2 (no eviction needed)"}}
+        if cap == "mlp":
+            r["network_evaluations_per_step"] = (s1["cap_mlp"] - s0["cap_mlp"]) / (steps - 16)
+            r["formula_fallback_fraction"] = (s1["cap_fallback"] - s0["cap_fallback"]) / max(
+                1, (s1["cap_mlp"] - s0["cap_mlp"]) + (s1["cap_fallback"] - s0["cap_fallback"]))
+            r["closure_error_final_bed"] = closure_error(e, net)
+        out[name] = r
+        e.close()
+        torch.cuda.empty_cache()
+    sub = None
+    if which == "wet16m":
+        ws_ = configs.wet(n=1_000_000, cyl_r=37.5e-3, steps=steps)
+        sub = {"particles": ws_.setup.n, "cyl_r_m": 37.5e-3, "steps": steps}
+        for name, prec, cap in (("mixed_mlp", "mixed", "mlp"), ("fp64", "fp64", "formula")):
+            e = Engine(ws_.setup, precision=prec, capillary=cap)
+            if cap == "mlp":
+                e.set_capnet(net)
+            e.set_state(ws_.pos0_reduced)
+            dt, _ = run_span(e, steps)
+            m = packing_metrics(ws_.setup, e.get_state()["pos"])
+            sub[name] = {"particle_steps_per_s": ws_.setup.n * steps / dt, "phi": m["phi"], "z": m["z"],
+                         "n_probe": m["n_probe"]}
+            e.close()
+        sub["phi_rel_err"] = abs(sub["mixed_mlp"]["phi"] - sub["fp64"]["phi"]) / sub["fp64"]["phi"]
+        sub["z_rel_err"] = abs(sub["mixed_mlp"]["z"] - sub["fp64"]["z"]) / max(sub["fp64"]["z"], 1e-300)
+    net.close()
+    print(json.dumps({
+        "metric": "particle-steps/s, wet spheres, fused learned capillary closure", "workload": which,
+        "unit": UNIT, "particles": n, "steps": steps, "dt_s": 5e-7, "cyl_r_m": r_big,
+        "data": "synthetic (seeded deposited bed, log-normal sizes)", "generate_s": t_gen,
+        "timing": "host wall time around one graph-replayed span of steps after 16 warm-up, rebuilds included",
+        "closure_training": {"samples": used, "epochs": rep["epochs"], "fit_seconds": rep["seconds"],
+                             "bed": "200,000-sphere wet bed while settling"},
+        "memory_plan": fit, "runs": out, "sub_cylinder_vs_fp64": sub}), flush=True)
+
+
+def step_kernel(pairs: str, capillary: str = "formula") -> str:
+    """the step kernel the library launches for this pair loop and closure"""
+    thread = pairs == "thread" or (pairs == "auto" and capillary == "mlp")
+    return ("k_step_mixed" if thread else "k_step_coop") + ("<1,1>" if capillary == "mlp" else "<1,0>")
+
+
+def traffic_from_profiles(kernel: str) -> float | None:
     """DRAM bytes per launch of the fused step kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "step_mixed_wet200k.md"
+    name = "step_mixed_wet200k.md" if kernel.startswith("k_step_mixed") else "step_coop_wet200k.md"
+    p = ROOT / "profiles" / name
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -321,9 +556,18 @@ def main():
     ap.add_argument("--host-steps", action="store_true",
                     help="launch every step's kernels directly instead of from CUDA graphs (for ncu, which "
                          "cannot profile kernels of graphs with conditional nodes)")
-    ap.add_argument("--workload", default="wet200k", choices=["wet200k", "dry5k", "ensemble"],
-                    help="wet200k: the headline bench; dry5k: the dry lattice packing run whole on GPU and CPU; "
-                         "ensemble: independent packings batched in one engine")
+    ap.add_argument("--workload", default="wet200k",
+                    choices=["wet200k", "wet200k-full", "dry5k", "ensemble", "wet2m", "wet16m"],
+                    help="wet200k: the headline bench; wet200k-full: the wet bed's whole run, FP64 against the "
+                         "fast paths; dry5k: the dry lattice packing run whole on GPU and CPU; ensemble: "
+                         "independent packings batched in one engine; wet2m / wet16m: large wet beds with the "
+                         "fused learned closure")
+    ap.add_argument("--pairs", default="auto", choices=["auto", "warp", "thread"],
+                    help="pair loop of the step kernel: warp-cooperative, one thread per particle, or auto (the "
+                         "library's default: warp with the capillary formula, thread with the learned closure)")
+    ap.add_argument("--block-size", type=int, default=0, help="threads per block of the step kernel (0: default)")
+    ap.add_argument("--full-steps", type=int, default=50000)
+    ap.add_argument("--large-steps", type=int, default=0, help="steps of wet2m / wet16m (0: 10,000 / 5,000)")
     ap.add_argument("--dry-steps", type=int, default=20000)
     ap.add_argument("--ens-systems", type=int, default=256)
     ap.add_argument("--ens-steps", type=int, default=10000)
@@ -341,6 +585,14 @@ def main():
     if args.workload == "ensemble":
         if rank == 0:
             run_ensemble(args)
+        return
+    if args.workload == "wet200k-full":
+        if rank == 0:
+            run_wet_full(args)
+        return
+    if args.workload in ("wet2m", "wet16m"):
+        if rank == 0:
+            run_wet_large(args, args.workload)
         return
 
     import torch
@@ -361,7 +613,8 @@ def main():
 
     from gpucode_gb300._abi import check, ptr
 
-    eng = Engine(w.setup, precision="mixed", use_graph=not args.host_steps, graph_steps=1)
+    eng = Engine(w.setup, precision="mixed", use_graph=not args.host_steps, graph_steps=1, pairs=args.pairs,
+                 block_size=args.block_size)
     eng.set_state(w.pos0_reduced)
     stream = torch.cuda.ExternalStream(eng.stream())
     # L2 eviction between timed steps: write 256 MB, then read another 256 MB,
@@ -445,7 +698,8 @@ def main():
                                    C.byref(ms_k)), "dem_profile_step")
     peak, peak_kind = _peaks()
     achieved = n * bytes_per_particle / (ms_k.value * 1e-3) / 1e9
-    traffic = traffic_from_profiles()
+    kname = step_kernel(args.pairs)
+    traffic = traffic_from_profiles(kname)
 
     # end to end through the public API with host buffers: H2D state, one step, D2H state + force
     hp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
@@ -499,7 +753,8 @@ def main():
         xs, ys = [], []
         net = cn.CapNet(seed=0)
         rep = net.fit(x, y, epochs=args.capnet_epochs, batch=8192, lr=1e-3, val_frac=0.1, seed=2024)
-        em = Engine(w.setup, precision="mixed", capillary="mlp", graph_steps=1)
+        em = Engine(w.setup, precision="mixed", capillary="mlp", graph_steps=1, pairs=args.pairs,
+                    block_size=args.block_size)
         em.set_capnet(net)
         em.set_state(w.pos0_reduced)
         em.step(args.settle + args.warmup)
@@ -588,14 +843,15 @@ def main():
             "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32-force/f64-state", "data": "synthetic (seeded deposited bed, log-normal sizes)",
             "config": {"workload": "wet200k", "particles": n, "levels": int(w.setup.s.n_levels), "dt_s": 5e-7,
-                       "capillary": "formula", "parallelism": "replicas" if ws > 1 else "single",
+                       "capillary": "formula", "pair_loop": args.pairs,
+                       "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "evicted between timed steps (256 MB write + 256 MB read, outside the per-step events)",
                        "per_step_counts": {"n_nb": n_nb, "n_c": n_c, "n_w": n_w, "n_wall": n_wall,
                                            "rebuilds": d["rebuilds"]},
                        "wall_s": t_wall},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_step_mixed (fused contact + capillary + wall + integrate)",
+                         "kernel": kname + " (fused contact + capillary + wall + integrate)",
                          "bytes_per_particle": bytes_per_particle, "kernel_ms": ms_k.value},
             "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": cpu_sample},

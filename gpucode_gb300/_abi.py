@@ -32,6 +32,9 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 CAP_FORMULA = 0
 CAP_MLP = 1
+PAIRS_AUTO = 0
+PAIRS_WARP = 1
+PAIRS_THREAD = 2
 
 
 class double3(C.Structure):
@@ -121,7 +124,7 @@ class DemSetup(C.Structure):
 
 class DemOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("capillary", C.c_int), ("block_size", C.c_int), ("reorder", C.c_int),
-                ("use_graph", C.c_int), ("graph_steps", C.c_int)]
+                ("use_graph", C.c_int), ("graph_steps", C.c_int), ("pair_mode", C.c_int)]
 
 
 class DemStats(C.Structure):

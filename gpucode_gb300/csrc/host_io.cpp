@@ -698,23 +698,45 @@ extern "C" dem_status dem_pack_deposit(int n, const double* dia, double cx, doub
       const double x = cx + rad * std::cos(th), y = cy + rad * std::sin(th);
       double z = z0 + ri + gap;
       const int ix = (int)((x - x0) / cell), iy = (int)((y - y0) / cell);
+      /* the 9 buckets around the drop point, walked together from the highest
+       * top down: the first spheres met are the ones the drop lands on, and
+       * the walk ends when the next top is too low to raise the landing
+       * height (each bucket alone would be scanned to the floor whenever the
+       * drop misses its upper spheres) */
+      const std::vector<int>* B[9];
+      size_t head[9];
+      int nb = 0;
       for (int dy = -1; dy <= 1; dy++)
         for (int dx = -1; dx <= 1; dx++) {
           const int bxi = ix + dx, byi = iy + dy;
           if (bxi < 0 || byi < 0 || bxi >= g || byi >= g) continue;
           const std::vector<int>& L = bucket[(size_t)byi * g + bxi];
-          for (size_t r = L.size(); r-- > 0;) {
-            const int j = L[r];
-            /* the highest landing height sphere j can give is its top + ri + gap */
-            if (top_of(j) + ri + gap <= z) break;
-            const double reach = ri + 0.5 * dia[j] + gap;
-            const double hx = x - pos_out[j].x, hy = y - pos_out[j].y;
-            const double h2 = hx * hx + hy * hy;
-            if (h2 >= reach * reach) continue;
-            const double zc = pos_out[j].z + std::sqrt(reach * reach - h2);
-            if (zc > z) z = zc;
+          if (L.empty()) continue;
+          B[nb] = &L;
+          head[nb] = L.size();
+          nb++;
+        }
+      for (;;) {
+        int pick = -1;
+        double best_top = -1e300;
+        for (int b = 0; b < nb; b++) {
+          if (head[b] == 0) continue;
+          const double t = top_of((*B[b])[head[b] - 1]);
+          if (t > best_top) {
+            best_top = t;
+            pick = b;
           }
         }
+        /* the highest landing height sphere j can give is its top + ri + gap */
+        if (pick < 0 || best_top + ri + gap <= z) break;
+        const int j = (*B[pick])[--head[pick]];
+        const double reach = ri + 0.5 * dia[j] + gap;
+        const double hx = x - pos_out[j].x, hy = y - pos_out[j].y;
+        const double h2 = hx * hx + hy * hy;
+        if (h2 >= reach * reach) continue;
+        const double zc = pos_out[j].z + std::sqrt(reach * reach - h2);
+        if (zc > z) z = zc;
+      }
       if (z < best_z) {
         best_z = z;
         bx = x;

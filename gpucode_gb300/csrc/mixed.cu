@@ -332,12 +332,10 @@ __device__ __forceinline__ uint32_t cap_pair(const CapNetSmem& w, const CapEntry
   return cap_pair(w, e.sep, e.vol, e.theta, e.ratio, t);
 }
 
-/* Run the queued bridges of this warp through the network (16-row BF16
- * tensor-core tiles), then let every lane fold in its own bridges, walking
- * its chain of entries from the newest: rupture decision, bridge flag,
- * force.  All 32 lanes call it; `last` is the lane's newest entry (-1: none). */
-__device__ __forceinline__ void cap_flush(const CapNetSmem& w, CapEntry* qw, int qn, int last, unsigned char* brg,
-                                          KSum3& F, int& wet, unsigned& nbr, unsigned& nmlp) {
+/* Run the queued bridges of this warp through the network in 16-row BF16
+ * tensor-core tiles; each entry's sep / vol fields receive the two outputs
+ * (normalised force, rupture distance).  All 32 lanes call it. */
+__device__ __forceinline__ void cap_run_queue(const CapNetSmem& w, CapEntry* qw, int qn) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   __syncwarp();
   for (int t0 = 0; t0 < qn; t0 += 16) {
@@ -362,6 +360,15 @@ __device__ __forceinline__ void cap_flush(const CapNetSmem& w, CapEntry* qw, int
     }
     __syncwarp();
   }
+}
+
+/* Run the queue through the network, then let every lane fold in its own
+ * bridges, walking its chain of entries from the newest: rupture decision,
+ * bridge flag, force.  All 32 lanes call it; `last` is the lane's newest
+ * entry (-1: none). */
+__device__ __forceinline__ void cap_flush(const CapNetSmem& w, CapEntry* qw, int qn, int last, unsigned char* brg,
+                                          KSum3& F, int& wet, unsigned& nbr, unsigned& nmlp) {
+  cap_run_queue(w, qw, qn);
   for (int e = last; e >= 0;) {
     const CapEntry& en = qw[e];
     e = (en.meta >> 8) - 1;
@@ -375,6 +382,128 @@ __device__ __forceinline__ void cap_flush(const CapNetSmem& w, CapEntry* qw, int
     }
   }
   __syncwarp();
+}
+
+/* After the pair loop, per particle: the <= 3 cylinder-wall contacts
+ * (CirPWInterG, kernel.cu:958-1023), the integrator (UpdateSystemG,
+ * kernel.cu:563-606), the next step's shadows and the counters. */
+template <bool NET>
+__device__ __forceinline__ void finish_particle(const MixArgs& a, int q, int qq, bool live, int sys, float4 hi,
+                                                float4 lo, float4 wi4, float3 iv, float3 iw, float ri, float twor,
+                                                float mass_f, KSum3& F, KSum3& M, KSum& R, int wet, unsigned nn,
+                                                unsigned ncont, unsigned nbr, unsigned nmlp, unsigned nfall) {
+  /* cylinder walls (CirPWInterG), geometry in FP64 */
+  unsigned nwc = 0;
+  double3 p = a.pos[qq];
+  const int nw = live ? a.nwall[qq] : 0;
+  if (nw > 0) {
+    const double rid = a.rad[qq];
+    const CylinderBC cy = a.cyl[sys];
+    double3 jvel = make_double3(0.0, 0.0, 0.0);
+    for (int w = 0; w < nw; w++) {
+      const int kind = a.wlist[3 * qq + w];
+      double3 jp;
+      if (kind == 0) {
+        jp = make_double3(p.x, p.y, cy.Tw);
+        jvel = make_double3(0.0, 0.0, cy.topv);
+      } else if (kind == 1) {
+        jp = make_double3(p.x, p.y, cy.Bw);
+      } else if (kind == 2) {
+        const double ddx = cy.cir.x - p.x, ddy = cy.cir.y - p.y;
+        const double dist = sqrt(ddx * ddx + ddy * ddy);
+        jp = make_double3(cy.R * ((p.x - cy.cir.x) / dist) + cy.cir.x, cy.R * ((p.y - cy.cir.y) / dist) + cy.cir.y,
+                          p.z);
+      } else {
+        continue;
+      }
+      const double3 d = make_double3(p.x - jp.x, p.y - jp.y, p.z - jp.z);
+      const double len = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+      const float gapw = (float)(len - rid);
+      if (gapw < 0.f) {
+        const float il = (float)(1.0 / len);
+        const float3 u = f3((float)d.x * il, (float)d.y * il, (float)d.z * il);
+        const float3 cpv = (iv - f3((float)jvel.x, (float)jvel.y, (float)jvel.z)) - crossf(iw * ri, u);
+        ContactRec* rp = a.wrec + (long long)w * a.n + qq;
+        MixedRec rc = load_rec(rp);
+        float3 dF, dM;
+        float dR;
+        law32(a.pw, ri, -gapw, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
+        store_rec(rp, rc);
+        F.add(dF);
+        M.add(dM);
+        R.add(dR);
+        nwc++;
+      }
+    }
+  }
+
+  /* integrator (UpdateSystemG) in FP64 with FP32 increments */
+  bool flagged = false;
+  if (live) {
+    /* 13 FP64 operations per particle: v += dv (3), x += v dt (3), path
+     * length (1), spin (3), binade shift of the shadow (3); every conversion
+     * goes through the integer pipe */
+    const float fx = F.x.s - F.x.c, fy = F.y.s - F.y.c, fz = F.z.s - F.z.c;
+    const float inv_m = a.dtf / mass_f;
+    double3 v = a.vel[q];
+    v.x += f2d(fx * inv_m);
+    v.y += f2d(fy * inv_m);
+    v.z += f2d(fz * inv_m);
+    p.x = fma(v.x, a.dt, p.x);
+    p.y = fma(v.y, a.dt, p.y);
+    p.z = fma(v.z, a.dt, p.z);
+    const float vxf = d2f(v.x), vyf = d2f(v.y), vzf = d2f(v.z);
+    const double pm = a.pmove[q] + f2d(sqrtf(vxf * vxf + vyf * vyf + vzf * vzf) * a.dtf);
+    const float inert = 0.1f * mass_f * twor * twor;
+    const float inv_i = a.dtf / inert;
+    double3 w = a.angv[q];
+    /* spin: w += M dt / I, then the rolling-resistance damping
+     * w *= 1 - min(1, Mr dt / I / |w|), folded into one increment */
+    const float dwx = (M.x.s - M.x.c) * inv_i, dwy = (M.y.s - M.y.c) * inv_i, dwz = (M.z.s - M.z.c) * inv_i;
+    const float rm = (R.s - R.c) * inv_i;
+    const float wx1 = wi4.x + dwx, wy1 = wi4.y + dwy, wz1 = wi4.z + dwz;
+    const float wl = sqrtf(wx1 * wx1 + wy1 * wy1 + wz1 * wz1);
+    float ix = dwx, iy = dwy, iz = dwz;
+    if (wl > 1.0e-7f) {
+      const float f = fminf(1.0f, rm / wl);
+      ix -= wx1 * f;
+      iy -= wy1 * f;
+      iz -= wz1 * f;
+    }
+    w.x += f2d(ix);
+    w.y += f2d(iy);
+    w.z += f2d(iz);
+    a.vel[q] = v;
+    a.pos[q] = p;
+    a.angv[q] = w;
+    a.pmove[q] = pm;
+    flagged = pm > a.move_limit;
+    if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(a.err, 2);
+    /* next step's shadows */
+    float4 ph, pl;
+    split_hi_lo(p.x + a.off.x, a.bin_exp, a.lo_scale, ph.x, pl.x);
+    split_hi_lo(p.y + a.off.y, a.bin_exp, a.lo_scale, ph.y, pl.y);
+    split_hi_lo(p.z + a.off.z, a.bin_exp, a.lo_scale, ph.z, pl.z);
+    ph.w = hi.w;
+    pl.w = lo.w;
+    a.phi_out[q] = ph;
+    a.plo_out[q] = pl;
+    a.v_out[q] = make_float4(vxf, vyf, vzf, __int_as_float(wet));
+    a.w_out[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
+    a.force_out[q] = make_float4(fx, fy, fz, 0.f);
+  }
+  const unsigned fm = __ballot_sync(0xffffffffu, flagged);
+  if ((threadIdx.x & 31) == 0 && fm) atomicAdd(a.flag, __popc(fm));
+  if (a.counters) {
+    warp_add(&a.counters[0], (unsigned)nn);
+    warp_add(&a.counters[1], ncont);
+    warp_add(&a.counters[2], nbr);
+    warp_add(&a.counters[3], nwc);
+    if (NET) {
+      warp_add(&a.counters[5], nmlp);
+      warp_add(&a.counters[6], nfall);
+    }
+  }
 }
 
 template <bool WET, bool NET>
@@ -557,118 +686,443 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
   }
   if (NET && qn > 0) cap_flush(*capw, qw, qn, last, a.brg, F, wet, nbr, nmlp);
 
-  /* cylinder walls (CirPWInterG), geometry in FP64 */
-  unsigned nwc = 0;
-  double3 p = a.pos[qq];
-  const int nw = live ? a.nwall[qq] : 0;
-  if (nw > 0) {
-    const double rid = a.rad[qq];
-    const CylinderBC cy = a.cyl[sys];
-    double3 jvel = make_double3(0.0, 0.0, 0.0);
-    for (int w = 0; w < nw; w++) {
-      const int kind = a.wlist[3 * qq + w];
-      double3 jp;
-      if (kind == 0) {
-        jp = make_double3(p.x, p.y, cy.Tw);
-        jvel = make_double3(0.0, 0.0, cy.topv);
-      } else if (kind == 1) {
-        jp = make_double3(p.x, p.y, cy.Bw);
-      } else if (kind == 2) {
-        const double ddx = cy.cir.x - p.x, ddy = cy.cir.y - p.y;
-        const double dist = sqrt(ddx * ddx + ddy * ddy);
-        jp = make_double3(cy.R * ((p.x - cy.cir.x) / dist) + cy.cir.x, cy.R * ((p.y - cy.cir.y) / dist) + cy.cir.y,
-                          p.z);
-      } else {
-        continue;
-      }
-      const double3 d = make_double3(p.x - jp.x, p.y - jp.y, p.z - jp.z);
-      const double len = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
-      const float gapw = (float)(len - rid);
-      if (gapw < 0.f) {
-        const float il = (float)(1.0 / len);
-        const float3 u = f3((float)d.x * il, (float)d.y * il, (float)d.z * il);
-        const float3 cpv = (iv - f3((float)jvel.x, (float)jvel.y, (float)jvel.z)) - crossf(iw * ri, u);
-        ContactRec* rp = a.wrec + (long long)w * a.n + qq;
-        MixedRec rc = load_rec(rp);
-        float3 dF, dM;
-        float dR;
-        law32(a.pw, ri, -gapw, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
-        store_rec(rp, rc);
-        F.add(dF);
-        M.add(dM);
-        R.add(dR);
-        nwc++;
-      }
-    }
-  }
+  finish_particle<NET>(a, q, qq, live, sys, hi, lo, wi4, iv, iw, ri, twor, mass_f, F, M, R, wet, (unsigned)nn, ncont,
+                       nbr, nmlp, nfall);
+}
 
-  /* integrator (UpdateSystemG) in FP64 with FP32 increments */
-  bool flagged = false;
-  if (live) {
-    /* 13 FP64 operations per particle: v += dv (3), x += v dt (3), path
-     * length (1), spin (3), binade shift of the shadow (3); every conversion
-     * goes through the integer pipe */
-    const float fx = F.x.s - F.x.c, fy = F.y.s - F.y.c, fz = F.z.s - F.z.c;
-    const float inv_m = a.dtf / mass_f;
-    double3 v = a.vel[q];
-    v.x += f2d(fx * inv_m);
-    v.y += f2d(fy * inv_m);
-    v.z += f2d(fz * inv_m);
-    p.x = fma(v.x, a.dt, p.x);
-    p.y = fma(v.y, a.dt, p.y);
-    p.z = fma(v.z, a.dt, p.z);
-    const float vxf = d2f(v.x), vyf = d2f(v.y), vzf = d2f(v.z);
-    const double pm = a.pmove[q] + f2d(sqrtf(vxf * vxf + vyf * vyf + vzf * vzf) * a.dtf);
-    const float inert = 0.1f * mass_f * twor * twor;
-    const float inv_i = a.dtf / inert;
-    double3 w = a.angv[q];
-    /* spin: w += M dt / I, then the rolling-resistance damping
-     * w *= 1 - min(1, Mr dt / I / |w|), folded into one increment */
-    const float dwx = (M.x.s - M.x.c) * inv_i, dwy = (M.y.s - M.y.c) * inv_i, dwz = (M.z.s - M.z.c) * inv_i;
-    const float rm = (R.s - R.c) * inv_i;
-    const float wx1 = wi4.x + dwx, wy1 = wi4.y + dwy, wz1 = wi4.z + dwz;
-    const float wl = sqrtf(wx1 * wx1 + wy1 * wy1 + wz1 * wz1);
-    float ix = dwx, iy = dwy, iz = dwz;
-    if (wl > 1.0e-7f) {
-      const float f = fminf(1.0f, rm / wl);
-      ix -= wx1 * f;
-      iy -= wy1 * f;
-      iz -= wz1 * f;
-    }
-    w.x += f2d(ix);
-    w.y += f2d(iy);
-    w.z += f2d(iz);
-    a.vel[q] = v;
-    a.pos[q] = p;
-    a.angv[q] = w;
-    a.pmove[q] = pm;
-    flagged = pm > a.move_limit;
-    if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(a.err, 2);
-    /* next step's shadows */
-    float4 ph, pl;
-    split_hi_lo(p.x + a.off.x, a.bin_exp, a.lo_scale, ph.x, pl.x);
-    split_hi_lo(p.y + a.off.y, a.bin_exp, a.lo_scale, ph.y, pl.y);
-    split_hi_lo(p.z + a.off.z, a.bin_exp, a.lo_scale, ph.z, pl.z);
-    ph.w = hi.w;
-    pl.w = lo.w;
-    a.phi_out[q] = ph;
-    a.plo_out[q] = pl;
-    a.v_out[q] = make_float4(vxf, vyf, vzf, __int_as_float(wet));
-    a.w_out[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
-    a.force_out[q] = make_float4(fx, fy, fz, 0.f);
+/* ---------------- the warp-cooperative pair loop ----------------
+ * One thread per particle makes a warp walk max(nn) neighbour slots with most
+ * lanes idle (measured: 15 of 32 lanes active on the settled 200k wet bed) and
+ * issue the whole slot body -- geometry, contact law, bridge -- once per slot
+ * whatever each lane needs.  Here the 32 particles of a warp put their slots
+ * end to end (inclusive shuffle scan of the slot counts) and each pass over up
+ * to kChunk of them runs in phases, every lane taking the next item whichever
+ * particle owns it (binary search of the scan, in shuffles):
+ *   A  geometry of every pair (one 16-byte gather per partner, the exact
+ *      overlap for candidates); contacts and bridges are ballot-compacted into
+ *      two lists in shared memory;
+ *   B  the contact law over the compacted contacts only (velocity, spin and
+ *      the 64-byte record gathered together);
+ *   C  the capillary bridges over the compacted bridge list (formula, or the
+ *      learned closure's queue on the tensor cores);
+ *   D  every lane folds its own particle's pairs, in neighbour order, into its
+ *      Kahan sums.
+ * so the contact law issues once per 32 contacts rather than once per 32
+ * slots.  Then each lane finishes its particle (walls, integrator) as before. */
+
+struct PairOut {
+  float fx, fy, fz, mx, my, mz, rr;
+  int flags;
+};
+enum : int { kPContact = 1, kPWet = 2, kPNbr = 4, kPMlp = 8, kPFall = 16 };
+
+/* phase A's result for one pair */
+struct PairGeo {
+  float ux, uy, uz, gap;
+  int j;
+  float rj;
+  int meta;
+  int pad;
+};
+enum : int { kGContact = 1, kGBridge = 2, kGForm = 4 };
+
+/* the warp's 32 particles as the pair lanes read them */
+struct WarpOwn {
+  float4 hi[32], lo[32];
+  float4 v[32]; /* velocity, liquid volume */
+  float4 w[32]; /* spin, contact angle (learned closure) */
+  long long base[32];
+  int stride[32];
+};
+static_assert(sizeof(WarpOwn) % 16 == 0, "WarpOwn keeps 16-byte alignment");
+
+/* a lane's running sums and counts between passes (in shared memory, so
+ * that they hold no registers while the pairs are evaluated) */
+struct LaneAcc {
+  KSum3 F, M;
+  KSum R;
+  int wet;
+  unsigned ncont, nbr, nmlp, nfall, pad;
+};
+static_assert(sizeof(LaneAcc) == 80, "LaneAcc is 80 bytes");
+
+#ifndef DEM_COOP_CHUNK
+#define DEM_COOP_CHUNK 64
+#endif
+
+/* pairs per warp per pass (the learned closure's bridge queue holds a pass,
+ * so it never has to be flushed inside one) and the per-warp shared memory:
+ * own particles, lane sums, pair geometry and results, the two lists, queue */
+template <bool NET>
+struct Coop {
+  static constexpr int kChunk = NET ? 64 : DEM_COOP_CHUNK;
+  static constexpr size_t kOffAcc = sizeof(WarpOwn);
+  static constexpr size_t kOffGeo = kOffAcc + 32 * sizeof(LaneAcc);
+  static constexpr size_t kOffOut = kOffGeo + sizeof(PairGeo) * kChunk;
+  static constexpr size_t kOffQ = kOffOut + sizeof(PairOut) * kChunk;
+  static constexpr size_t kOffList = kOffQ + (NET ? sizeof(CapEntry) * kChunk : 0);
+  static constexpr size_t kWarpBytes = kOffList + 2 * kChunk;
+  static constexpr size_t smem(int warps) {
+    return (NET ? ((sizeof(CapNetSmem) + 15) / 16) * 16 : 0) + warps * kWarpBytes;
   }
-  const unsigned fm = __ballot_sync(0xffffffffu, flagged);
-  if ((threadIdx.x & 31) == 0 && fm) atomicAdd(a.flag, __popc(fm));
-  if (a.counters) {
-    warp_add(&a.counters[0], (unsigned)nn);
-    warp_add(&a.counters[1], ncont);
-    warp_add(&a.counters[2], nbr);
-    warp_add(&a.counters[3], nwc);
-    if (NET) {
-      warp_add(&a.counters[5], nmlp);
-      warp_add(&a.counters[6], nfall);
-    }
+  static_assert(kChunk % 32 == 0 && kChunk <= 256, "a pass is whole rounds of 32; list entries are bytes");
+  static_assert(kWarpBytes % 16 == 0 && kOffQ % 16 == 0, "per-warp areas keep 16-byte alignment");
+};
+
+#ifndef DEM_COOP_BLOCKS
+#define DEM_COOP_BLOCKS 6
+#endif
+
+/* the particle (lane) owning pair p: the number of lanes whose inclusive slot
+ * count is <= p.  Every lane of the warp calls it. */
+__device__ __forceinline__ int coop_owner(int incl, int p) {
+  int o = 0;
+#pragma unroll
+  for (int b = 16; b > 0; b >>= 1) {
+    const int v = __shfl_sync(0xffffffffu, incl, o + b - 1);
+    if (v <= p) o += b;
   }
+  return o;
+}
+
+/* phase A for one pair (owner o, partner j with coarse shadow hj): the
+ * overlap -- coarse from the hi parts, exact (hi + lo, error-free
+ * transforms) for candidates -- and what the later phases need */
+template <bool WET>
+__device__ __forceinline__ PairGeo coop_geo(const MixArgs& a, const WarpOwn& ow, int o, bool wet_o, long long s,
+                                            int j, float4 hj) {
+  PairGeo g;
+  const float4 hi = ow.hi[o], lo = ow.lo[o];
+  const float ax = hi.x - hj.x, ay = hi.y - hj.y, az = hi.z - hj.z; /* exact */
+  const float coarse = sqrtf(ax * ax + ay * ay + az * az) - (hi.w + hj.w);
+  g.gap = coarse;
+  g.ux = g.uy = g.uz = 0.f;
+  g.rj = hj.w;
+  g.j = j;
+  g.meta = 0;
+  g.pad = 0;
+  if (WET || coarse < a.coarse_tol) {
+    const float4 lj = ro(a.plo_in + j);
+    g.rj = hj.w + lj.w;
+    const float bx = lo.x - lj.x, by = lo.y - lj.y, bz = lo.z - lj.z;
+    /* d^2 - S^2 from exact pieces */
+    const float px = ax * ax, py = ay * ay, pz = az * az;
+    const float ex = fmaf(ax, ax, -px), ey = fmaf(ay, ay, -py), ez = fmaf(az, az, -pz);
+    float t1, t2, es;
+    const float s1 = two_sum(px, py, t1);
+    const float s2 = two_sum(s1, pz, t2);
+    const float slo = (lo.w + lj.w);
+    const float Sh = two_sum(hi.w, hj.w, es);
+    const float Sl = es + slo;
+    const float qq2 = Sh * Sh, eq = fmaf(Sh, Sh, -qq2);
+    const float s3 = s2 - qq2;
+    const float small = (t1 + t2) + (ex + ey + ez - eq) + 2.0f * (ax * bx + ay * by + az * bz) -
+                        2.0f * Sh * Sl + (bx * bx + by * by + bz * bz) - Sl * Sl;
+    const float D = s3 + small;
+    const float dx = ax + bx, dy = ay + by, dz = az + bz;
+    const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+    g.gap = __fdividef(D, dist + (Sh + Sl));
+    const float inv = __frcp_rn(dist);
+    g.ux = dx * inv;
+    g.uy = dy * inv;
+    g.uz = dz * inv;
+    if (g.gap < 0.f) g.meta = kGContact;
+  }
+  if (WET && wet_o) {
+    /* a bridge to evaluate: an existing one, or one forming this step (gap
+     * below the liquid layer); the others stay unbridged (flag 0) */
+    const float ri = hi.w + lo.w;
+    const bool form = g.gap < 2.0f * a.lqd_layer * (ri + g.rj);
+    if (form) g.meta |= kGBridge | kGForm;
+    else if (a.brg[s]) g.meta |= kGBridge;
+  }
+  return g;
+}
+
+/* phase B for one contact: the elasto-plastic law with its history record */
+__device__ __forceinline__ PairOut coop_contact(const MixArgs& a, const WarpOwn& ow, int o, long long s,
+                                                const PairGeo& g) {
+  const float4 vj4 = ro(a.v_in + g.j), wj4 = ro(a.w_in + g.j);
+  MixedRec rc = load_rec(a.rec + s);
+  const float4 hi = ow.hi[o], lo = ow.lo[o], vi = ow.v[o], wi = ow.w[o];
+  const float ri = hi.w + lo.w, rj = g.rj;
+  const float3 u = f3(g.ux, g.uy, g.uz);
+  const float3 cpv = (f3(vi.x - vj4.x, vi.y - vj4.y, vi.z - vj4.z)) -
+                     crossf(f3(wi.x, wi.y, wi.z) * ri + f3(wj4.x, wj4.y, wj4.z) * rj, u);
+  const float ijRad = ri * rj / (ri + rj);
+  float3 dF, dM;
+  float dR;
+  law32(a.pp, ijRad, -g.gap, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
+  store_rec(a.rec + s, rc);
+  return PairOut{dF.x, dF.y, dF.z, dM.x, dM.y, dM.z, dR, kPContact};
+}
+
+/* phase C for one bridge: rupture decision, bridge flag and force with the
+ * plain formula, added into the pair's result (NET: inside the network's
+ * training box the bridge is queued in `ent` instead, want = true) */
+template <bool NET>
+__device__ __forceinline__ void coop_bridge(const MixArgs& a, const WarpOwn& ow, int o, long long s,
+                                            const PairGeo& g, PairOut& out, const CapNetSmem* capw, int pidx,
+                                            bool& want, CapEntry& ent) {
+  const float4 hi = ow.hi[o], lo = ow.lo[o];
+  const float ri = hi.w + lo.w, rj = g.rj;
+  int jnl = __float_as_int(ro(a.v_in + g.j).w);
+  if (jnl < 12) jnl = 12;
+  const float tj = 2.0f * rj;
+  const float ijVol = ow.v[o].w + __fdividef(a.lqd_vol * (tj * tj * tj), (float)jnl);
+  const bool form = (g.meta & kGForm) != 0;
+  const float effR = 2.0f * ri * rj / (ri + rj);
+  const float vol = 8.0f * ijVol;
+  if (NET) {
+    const float sep = fmaxf(a.lqd_gapmn, fmaxf(g.gap, 0.f));
+    const float theta = 0.5f * (ow.w[o].w + cap_theta(ro(a.id + g.j), a.theta_seed, a.theta_max));
+    const float ratio = __fdividef(fminf(ri, rj), fmaxf(ri, rj));
+    if (cap_in_hull(*capw, sep, vol, theta, ratio) && s <= 0xffffffffLL) {
+      const float sc = -2.0f * kPiF * effR * a.lqd_st;
+      ent = CapEntry{sep, vol, theta, ratio, g.ux * sc, g.uy * sc, g.uz * sc, g.gap, (unsigned)s,
+                     (form ? 1 : 0) | (pidx << 8)};
+      want = true;
+      return;
+    }
+    out.flags |= kPFall;
+  }
+  const float rupture = 0.99f * exp2f(0.33f * __log2f(ijVol));
+  const int b = form ? 1 : (g.gap > rupture ? 0 : 1);
+  a.brg[s] = (unsigned char)b;
+  if (b) {
+    const float fc = fcap32(g.gap < 0.f ? 0.f : g.gap, vol, effR, a.lqd_gapmn, a.lqd_st);
+    out.fx -= g.ux * fc;
+    out.fy -= g.uy * fc;
+    out.fz -= g.uz * fc;
+    out.flags |= kPWet | (g.gap >= 0.f ? kPNbr : 0);
+  }
+}
+
+/* run the pass's bridge queue through the network, then fold each entry into
+ * its pair's result: rupture decision, bridge flag, force */
+__device__ __forceinline__ void cap_fold_coop(const CapNetSmem& w, CapEntry* qw, int qn, PairOut* pb,
+                                              unsigned char* brg) {
+  cap_run_queue(w, qw, qn);
+  for (int e = threadIdx.x & 31; e < qn; e += 32) {
+    const CapEntry en = qw[e];
+    const int b = (en.meta & 1) ? 1 : (en.gap > en.vol ? 0 : 1);
+    brg[en.slot] = (unsigned char)b;
+    PairOut& r = pb[en.meta >> 8];
+    int fl = r.flags | kPMlp;
+    if (b) {
+      r.fx += en.wx * en.sep;
+      r.fy += en.wy * en.sep;
+      r.fz += en.wz * en.sep;
+      fl |= kPWet | (en.gap >= 0.f ? kPNbr : 0);
+    }
+    r.flags = fl;
+  }
+  __syncwarp();
+}
+
+/* the slot of pair p of owner o */
+__device__ __forceinline__ long long coop_slot(const WarpOwn& ow, int o, int p, int eo) {
+  return ow.base[o] + (long long)(p - eo) * ow.stride[o];
+}
+
+template <bool WET, bool NET>
+__global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_step_coop(MixArgs a) {
+  if (a.n <= 0) return;
+  using CF = Coop<NET>;
+  constexpr int CH = CF::kChunk;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = q < a.n;
+  const int qq = live ? q : a.n - 1;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const CapNetSmem* capw = reinterpret_cast<const CapNetSmem*>(dsm);
+  unsigned char* wsm = dsm + (NET ? ((sizeof(CapNetSmem) + 15) / 16) * 16 : 0) + (threadIdx.x >> 5) * CF::kWarpBytes;
+  WarpOwn& ow = *reinterpret_cast<WarpOwn*>(wsm);
+  LaneAcc* acc = reinterpret_cast<LaneAcc*>(wsm + CF::kOffAcc);
+  PairGeo* geo = reinterpret_cast<PairGeo*>(wsm + CF::kOffGeo);
+  PairOut* pb = reinterpret_cast<PairOut*>(wsm + CF::kOffOut);
+  CapEntry* qw = reinterpret_cast<CapEntry*>(wsm + CF::kOffQ);
+  unsigned char* clist = wsm + CF::kOffList;
+  unsigned char* blist = clist + CH;
+  if (NET) {
+    cap_stage(a.capw, reinterpret_cast<CapNetSmem*>(dsm));
+    __syncthreads();
+  }
+  /* the integrator's FP64 state is needed only after the pair loop */
+  prefetch_l2(a.pos + qq);
+  prefetch_l2(a.vel + qq);
+  prefetch_l2(a.angv + qq);
+  prefetch_l2(a.pmove + qq);
+
+  const int sys = a.sys_of_id ? a.sys_of_id[ro(a.id + qq)] : 0;
+  const int nn = live ? ro(a.num_nebor + qq) : 0;
+  unsigned wetm;
+  {
+    /* this lane's particle, for the lanes that evaluate its pairs and for
+     * the integrator after the loop (read back from shared memory then) */
+    const float4 hi = ro(a.phi_in + qq), lo = ro(a.plo_in + qq), vi4 = ro(a.v_in + qq), wi4 = ro(a.w_in + qq);
+    const float twor = 2.0f * (hi.w + lo.w);
+    const float mass_f = twor * twor * twor;
+    const bool wet_i = WET && (!a.sys_wet || a.sys_wet[sys]);
+    float iVol = 0.f;
+    if (WET) {
+      int inl = __float_as_int(vi4.w);
+      if (inl < 12) inl = 12;
+      iVol = a.lqd_vol * mass_f / (float)inl;
+    }
+    const int L = ro(a.plevel + qq);
+    ow.hi[lane] = hi;
+    ow.lo[lane] = lo;
+    ow.v[lane] = make_float4(vi4.x, vi4.y, vi4.z, iVol);
+    ow.w[lane] = make_float4(wi4.x, wi4.y, wi4.z, NET ? cap_theta(ro(a.id + qq), a.theta_seed, a.theta_max) : 0.f);
+    ow.base[lane] = slot_base(L, a.npars, a.nneb) + ro(a.nidx + qq);
+    ow.stride[lane] = ro(a.npars + L);
+    LaneAcc z;
+    z.F = KSum3();
+    z.M = KSum3();
+    z.R = KSum();
+    z.F.z.add(-mass_f); /* gravity, m = (2r)^3 */
+    z.wet = 0;
+    z.ncont = z.nbr = z.nmlp = z.nfall = z.pad = 0;
+    acc[lane] = z;
+    wetm = __ballot_sync(FULL, wet_i);
+  }
+  /* the warp's slots end to end */
+  int incl = nn;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int excl = incl - nn;
+  const int total = __shfl_sync(FULL, incl, 31);
+  __syncwarp();
+
+  for (int c0 = 0; c0 < total; c0 += CH) {
+    const int cend = min(total, c0 + CH);
+    /* ---- A: geometry of every pair; contacts and bridges listed ---- */
+    int nc = 0, nb = 0;
+    {
+      /* pair p of this lane, and one round ahead: its partner index and
+       * coarse shadow are in flight while the current pair is evaluated */
+      int p = c0 + lane;
+      bool act = p < cend;
+      int o = coop_owner(incl, p);
+      long long s = 0;
+      int j = 0;
+      float4 hj = make_float4(0.f, 0.f, 0.f, 0.f);
+      {
+        const int eo = __shfl_sync(FULL, excl, o);
+        if (act) {
+          s = coop_slot(ow, o, p, eo);
+          j = ro(a.nebor + s);
+          hj = ro(a.phi_in + j);
+        }
+      }
+      for (int p0 = c0; p0 < cend; p0 += 32) {
+        const int pn = p + 32;
+        const bool actn = pn < cend;
+        const int on = coop_owner(incl, pn);
+        const int eon = __shfl_sync(FULL, excl, on);
+        long long sn = 0;
+        int jn = 0;
+        float4 hjn = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (actn) {
+          sn = coop_slot(ow, on, pn, eon);
+          jn = ro(a.nebor + sn);
+          hjn = ro(a.phi_in + jn);
+        }
+        int meta = 0;
+        if (act) {
+          const PairGeo g = coop_geo<WET>(a, ow, o, (wetm >> o) & 1u, s, j, hj);
+          geo[p - c0] = g;
+          meta = g.meta;
+        }
+        const unsigned mc = __ballot_sync(FULL, meta & kGContact);
+        const unsigned mb = __ballot_sync(FULL, meta & kGBridge);
+        if (meta & kGContact) clist[nc + __popc(mc & lt)] = (unsigned char)(p - c0);
+        if (meta & kGBridge) blist[nb + __popc(mb & lt)] = (unsigned char)(p - c0);
+        nc += __popc(mc);
+        nb += __popc(mb);
+        p = pn;
+        act = actn;
+        o = on;
+        s = sn;
+        j = jn;
+        hj = hjn;
+      }
+    }
+    __syncwarp();
+    /* ---- B: the contact law over the compacted contacts ---- */
+    for (int k0 = 0; k0 < nc; k0 += 32) {
+      const int k = k0 + lane;
+      const int pidx = k < nc ? clist[k] : 0;
+      const int p = c0 + pidx;
+      const int o = coop_owner(incl, p);
+      const int eo = __shfl_sync(FULL, excl, o);
+      if (k < nc) pb[pidx] = coop_contact(a, ow, o, coop_slot(ow, o, p, eo), geo[pidx]);
+    }
+    __syncwarp();
+    /* ---- C: the bridges over the compacted list ---- */
+    if (WET) {
+      int qn = 0;
+      for (int k0 = 0; k0 < nb; k0 += 32) {
+        const int k = k0 + lane;
+        const int pidx = k < nb ? blist[k] : 0;
+        const int p = c0 + pidx;
+        const int o = coop_owner(incl, p);
+        const int eo = __shfl_sync(FULL, excl, o);
+        bool want = false;
+        CapEntry ent;
+        if (k < nb) {
+          const PairGeo g = geo[pidx];
+          PairOut r;
+          if (g.meta & kGContact) r = pb[pidx];
+          else r = PairOut{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+          coop_bridge<NET>(a, ow, o, coop_slot(ow, o, p, eo), g, r, capw, pidx, want, ent);
+          pb[pidx] = r;
+        }
+        if (NET) {
+          const unsigned m = __ballot_sync(FULL, want);
+          if (want) qw[qn + __popc(m & lt)] = ent;
+          qn += __popc(m);
+        }
+      }
+      if (NET && qn > 0) cap_fold_coop(*capw, qw, qn, pb, a.brg);
+    }
+    __syncwarp();
+    /* ---- D: this lane's particle, its pairs of the pass in neighbour order ---- */
+    const int k0 = max(excl, c0), k1 = min(incl, cend);
+    if (k0 < k1) {
+      LaneAcc A = acc[lane];
+      for (int kk = k0; kk < k1; kk++) {
+        if (!(geo[kk - c0].meta & (kGContact | kGBridge))) continue;
+        const PairOut r = pb[kk - c0];
+        if (r.flags & (kPContact | kPWet)) A.F.add(f3(r.fx, r.fy, r.fz));
+        if (r.flags & kPContact) {
+          A.M.add(f3(r.mx, r.my, r.mz));
+          A.R.add(r.rr);
+          A.ncont++;
+        }
+        if (r.flags & kPWet) A.wet++;
+        if (r.flags & kPNbr) A.nbr++;
+        if (NET) {
+          if (r.flags & kPMlp) A.nmlp++;
+          if (r.flags & kPFall) A.nfall++;
+        }
+      }
+      acc[lane] = A;
+    }
+    __syncwarp();
+  }
+  LaneAcc A = acc[lane];
+  const float4 hi = ow.hi[lane], lo = ow.lo[lane], v = ow.v[lane], w = ow.w[lane];
+  const float ri = hi.w + lo.w, twor = 2.0f * ri;
+  const float4 wi4 = make_float4(w.x, w.y, w.z, 0.f);
+  finish_particle<NET>(a, q, qq, live, sys, hi, lo, wi4, f3(v.x, v.y, v.z), f3(w.x, w.y, w.z), ri, twor,
+                       twor * twor * twor, A.F, A.M, A.R, A.wet, (unsigned)nn, A.ncont, A.nbr, A.nmlp, A.nfall);
 }
 
 __global__ void k_shadows(int n, const double3* __restrict__ pos, const double3* __restrict__ vel,
@@ -725,7 +1179,25 @@ Law32 make_law(const calParaPP& c, bool pp, double dmp_sq, int stage) {
 
 }  // namespace
 
+#ifndef DEM_COOP_CARVEOUT
+#define DEM_COOP_CARVEOUT cudaSharedmemCarveoutMaxShared
+#endif
+
+template <class K>
+cudaError_t coop_attrs(K kernel, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && DEM_COOP_CARVEOUT >= 0)
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, DEM_COOP_CARVEOUT);
+  return e;
+}
+
 dem_status mixed_create(dem_ctx* c) {
+  /* the cooperative step kernels: shared memory above the default 48 KB per
+   * block, and the largest shared-memory carveout (set before any capture) */
+  cudaError_t e = coop_attrs(k_step_coop<true, true>, Coop<true>::smem(kWarps));
+  if (e == cudaSuccess) e = coop_attrs(k_step_coop<true, false>, Coop<false>::smem(kWarps));
+  if (e == cudaSuccess) e = coop_attrs(k_step_coop<false, false>, Coop<false>::smem(kWarps));
+  if (e != cudaSuccess) return cuda_check(e, "mixed_create kernel attributes");
   MixedState* m = new MixedState();
   std::memset(m, 0, sizeof(*m));
   c->mx = m;
@@ -814,13 +1286,18 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   /* threads per block: the option (a multiple of 32 up to 128), else 128 */
   const int ob = c->opt.block_size;
   const int bs = (ob >= 32 && ob <= 32 * kWarps && ob % 32 == 0) ? ob : 32 * kWarps;
-  if (c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP) {
-    if (!c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
-    k_step_mixed<true, true><<<grid_for(c->n, bs), bs, kCapSmem, s>>>(a);
-  } else if (c->s.force_cap == 1) {
-    k_step_mixed<true, false><<<grid_for(c->n, bs), bs, 0, s>>>(a);
+  const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;
+  if (net && !c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
+  const int g = grid_for(c->n, bs);
+  const bool thread_loop = c->opt.pair_mode == DEM_PAIRS_THREAD || (c->opt.pair_mode == DEM_PAIRS_AUTO && net);
+  if (thread_loop) {
+    if (net) k_step_mixed<true, true><<<g, bs, kCapSmem, s>>>(a);
+    else if (c->s.force_cap == 1) k_step_mixed<true, false><<<g, bs, 0, s>>>(a);
+    else k_step_mixed<false, false><<<g, bs, 0, s>>>(a);
   } else {
-    k_step_mixed<false, false><<<grid_for(c->n, bs), bs, 0, s>>>(a);
+    if (net) k_step_coop<true, true><<<g, bs, Coop<true>::smem(bs / 32), s>>>(a);
+    else if (c->s.force_cap == 1) k_step_coop<true, false><<<g, bs, Coop<false>::smem(bs / 32), s>>>(a);
+    else k_step_coop<false, false><<<g, bs, Coop<false>::smem(bs / 32), s>>>(a);
   }
   return cuda_check(cudaGetLastError(), "mixed_step launch");
 }

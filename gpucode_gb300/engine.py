@@ -81,7 +81,7 @@ class Setup:
 
 
 def _options(precision: str = "mixed", capillary: str = "formula", reorder: bool = True, use_graph: bool = True,
-             graph_steps: int = 0, block_size: int = 0) -> DemOptions:
+             graph_steps: int = 0, block_size: int = 0, pairs: str = "auto") -> DemOptions:
     lib = _abi.load()
     opt = DemOptions()
     lib.dem_default_options(C.byref(opt))
@@ -91,6 +91,7 @@ def _options(precision: str = "mixed", capillary: str = "formula", reorder: bool
     opt.use_graph = 1 if use_graph else 0
     opt.graph_steps = int(graph_steps)
     opt.block_size = int(block_size)
+    opt.pair_mode = {"auto": _abi.PAIRS_AUTO, "warp": _abi.PAIRS_WARP, "thread": _abi.PAIRS_THREAD}[pairs]
     return opt
 
 
@@ -110,10 +111,10 @@ class Engine:
     """One simulation on one GPU (dem_ctx)."""
 
     def __init__(self, setup: Setup, precision: str = "mixed", reorder: bool = True, use_graph: bool = True,
-                 capillary: str = "formula", graph_steps: int = 0, block_size: int = 0):
+                 capillary: str = "formula", graph_steps: int = 0, block_size: int = 0, pairs: str = "auto"):
         self.lib = _abi.load()
         self.setup = setup
-        opt = _options(precision, capillary, reorder, use_graph, graph_steps, block_size)
+        opt = _options(precision, capillary, reorder, use_graph, graph_steps, block_size, pairs)
         self.opt = opt
         h = C.c_void_p()
         check(self.lib.dem_create(C.byref(setup.s), ptr(setup.rad), ptr(setup.plevel), ptr(setup.nidx),

@@ -254,6 +254,11 @@ dem_status dem_build_setup(const dem_input* in, const double* dia, dem_setup* ou
 enum { DEM_PREC_FP64 = 0, DEM_PREC_MIXED = 1 };
 /* capillary closure */
 enum { DEM_CAP_FORMULA = 0, DEM_CAP_MLP = 1 };
+/* pair loop of the mixed step kernel: the warp's lanes share out its particles'
+ * pairs (WARP), or one thread walks one particle's pairs (THREAD); AUTO (the
+ * default) takes WARP with the capillary formula and THREAD with the learned
+ * closure, the faster of the two for each on the 200k wet bed */
+enum { DEM_PAIRS_AUTO = 0, DEM_PAIRS_WARP = 1, DEM_PAIRS_THREAD = 2 };
 
 typedef struct dem_options {
   int precision;          /* DEM_PREC_* */
@@ -262,6 +267,7 @@ typedef struct dem_options {
   int reorder;            /* 1: keep particles in cell order (default); 0: reference order */
   int use_graph;          /* 1: replay steps through a CUDA graph (default) */
   int graph_steps;        /* time steps per graph launch (0 = 16) */
+  int pair_mode;          /* mixed step kernel: DEM_PAIRS_AUTO (default), _WARP or _THREAD */
 } dem_options;
 
 typedef struct dem_ctx dem_ctx;

@@ -77,10 +77,10 @@ def test_inference_matches_the_oracle(cuda):
     net.close()
 
 
-def _wet_engine(steps, capillary="formula"):
+def _wet_engine(steps, capillary="formula", pairs="auto"):
     w = _workloads.small_wet()
     pos, vel, ang = _workloads.stirred(w, vscale=0.05, wscale=0.1)
-    eng = Engine(w.setup, precision="mixed", capillary=capillary)
+    eng = Engine(w.setup, precision="mixed", capillary=capillary, pairs=pairs)
     eng.set_state(pos, vel, ang)
     if steps:
         eng.step(steps)
@@ -168,12 +168,13 @@ def test_network_gains_over_the_reference_precision_formula(trained):
     assert rel < 0.05
 
 
-def test_engine_with_an_empty_training_box_is_the_formula_engine(cuda):
+@pytest.mark.parametrize("pairs", ["warp", "thread"])
+def test_engine_with_an_empty_training_box_is_the_formula_engine(cuda, pairs):
     """a network whose training box holds nothing sends every bridge to the
-    plain formula: the learned-closure kernel variant must then reproduce the
-    formula kernel bit for bit"""
-    w, ref, st = _wet_engine(0)
-    _, eng, _ = _wet_engine(0, capillary="mlp")
+    plain formula: the learned-closure variant of each pair loop must then
+    reproduce that loop's formula variant bit for bit"""
+    w, ref, st = _wet_engine(0, pairs=pairs)
+    _, eng, _ = _wet_engine(0, capillary="mlp", pairs=pairs)
     rng = np.random.default_rng(1)
     _, _, norm = _random_features(rng, 100)
     norm[12:16], norm[16:20] = 1.0, -1.0  # lo > hi: empty box

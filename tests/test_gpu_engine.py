@@ -43,14 +43,52 @@ def test_fp64_engine_lockstep(cuda, make, reorder):
     eng.close()
 
 
+@pytest.mark.parametrize("pairs", ["warp", "thread"])
 @pytest.mark.parametrize("make", [_workloads.small_dry, _workloads.small_wet])
-def test_mixed_engine_lockstep(cuda, make):
+def test_mixed_engine_lockstep(cuda, make, pairs):
     w = make()
     pos, vel, ang = _workloads.stirred(w)
-    eng = Engine(w.setup, precision="mixed")
+    eng = Engine(w.setup, precision="mixed", pairs=pairs)
     worst = _lockstep.run(eng, w, pos, vel, ang, steps=250, tol=MIXED_TOL, mismatch_budget=0.01)
     assert worst["rebuilds"] >= 2, worst
     eng.close()
+
+
+@pytest.mark.parametrize("make", [_workloads.small_dry, _workloads.small_wet])
+def test_pair_loops_agree(cuda, make):
+    """The warp-cooperative pair loop and the thread-per-particle one evaluate
+    the same pairs with the same FP32 formulas and sum them in the same
+    neighbour order, but each kernel's instruction selection is its own (FMA
+    contraction, approximate division), and a wet contact's and its bridge's
+    forces are added into one FP32 value before the Kahan sum.  One step from
+    the same state: forces agree to FP32 rounding, state to the rounding of
+    one FP32 increment, and the labels (contacts, bridges, flags) but for
+    comparisons that land on their turning point."""
+    w = make()
+    pos, vel, ang = _workloads.stirred(w)
+    a = Engine(w.setup, precision="mixed", pairs="warp")
+    b = Engine(w.setup, precision="mixed", pairs="thread")
+    for e in (a, b):
+        e.set_state(pos, vel, ang)
+        e.step(1)
+        e.sync()
+    sa, sb = a.get_state(), b.get_state()
+    scale = float(np.abs(sb["force"]).max())
+    assert float(np.abs(sa["force"] - sb["force"]).max()) <= 1e-6 * scale
+    for k, tol in (("pos", 1e-12), ("vel", 1e-6)):
+        assert np.allclose(sa[k], sb[k], rtol=0, atol=tol * max(1.0, float(np.abs(sb[k]).max()))), k
+    # labels: a comparison at its turning point may round either way in the
+    # two kernels; allowed on at most 0.5% of the contacts
+    mp = _lockstep.max_per(w)
+    ha, hb = a.history(mp), b.history(mp)
+    budget = max(1, int(0.005 * max(1, int(np.count_nonzero(hb[0][..., 7])))))
+    assert int(np.count_nonzero(ha[1] != hb[1])) <= budget  # bridge flags
+    assert int(np.count_nonzero(ha[0][..., 7] != hb[0][..., 7])) <= budget  # load stages
+    sa_, sb_ = a.stats(), b.stats()
+    for k in ("contacts", "bridges", "wall_contacts"):
+        assert abs(sa_[k] - sb_[k]) <= budget, k
+    a.close()
+    b.close()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
