@@ -798,8 +798,11 @@ dem_status dem_set_contact_angles(dem_ctx* c, float theta_max, unsigned long lon
   if (!c || !(theta_max >= 0.f)) return fail(DEM_ERR_ARG, "dem_set_contact_angles: bad arguments");
   c->theta_max = theta_max;
   c->theta_seed = seed;
-  for (int p = 0; p < 2; p++)
+  /* the captured step kernels hold the old angles: recapture */
+  for (int p = 0; p < 2; p++) {
     if (c->graph_exec[p]) { cudaGraphExecDestroy(c->graph_exec[p]); c->graph_exec[p] = nullptr; }
+    if (c->graph_one[p]) { cudaGraphExecDestroy(c->graph_one[p]); c->graph_one[p] = nullptr; }
+  }
   return DEM_OK;
 }
 

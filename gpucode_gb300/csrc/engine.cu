@@ -217,6 +217,20 @@ __global__ void k_import(int n, const int* __restrict__ id, const double3* __res
   angv[q] = has_w ? hw[i] : make_double3(0.0, 0.0, 0.0);
 }
 
+/* inv[id[q]] = q: the cell-order position of each caller index */
+__global__ void k_inverse(int n, const int* __restrict__ id, int* __restrict__ inv) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) inv[id[q]] = q;
+}
+
+/* dst[i] = src[inv[i]]: caller order, gathered from cell order and written in
+ * order, ready for one contiguous copy to the host */
+__global__ void k_export_gather(int n, const int* __restrict__ inv, const double3* __restrict__ src,
+                                double3* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[inv[i]];
+}
+
 __global__ void k_export(int n, const int* __restrict__ id, const double3* __restrict__ src, double3* __restrict__ dst) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -310,13 +324,15 @@ dem_status enqueue_step(dem_ctx* c, cudaStream_t s, int parity) {
 void destroy_graph(dem_ctx* c) {
   for (int p = 0; p < 2; p++) {
     if (c->graph_exec[p]) cudaGraphExecDestroy(c->graph_exec[p]);
+    if (c->graph_one[p]) cudaGraphExecDestroy(c->graph_one[p]);
     c->graph_exec[p] = nullptr;
+    c->graph_one[p] = nullptr;
   }
 }
 
 /* G steps: [decide -> IF(rebuild) -> step] x G; the mixed path's shadow
  * parity alternates from start_parity */
-dem_status build_graph(dem_ctx* c, int G, int start_parity) {
+dem_status build_graph(dem_ctx* c, int G, int start_parity, cudaGraphExec_t* out) {
   cudaStream_t cs;
   cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_check(e, "capture stream");
@@ -379,7 +395,7 @@ dem_status build_graph(dem_ctx* c, int G, int start_parity) {
   }
   if (st == DEM_OK) {
     cudaGraphExec_t ex = nullptr;
-    if (ck(cudaGraphInstantiate(&ex, g, 0), "cudaGraphInstantiate")) c->graph_exec[start_parity] = ex;
+    if (ck(cudaGraphInstantiate(&ex, g, 0), "cudaGraphInstantiate")) *out = ex;
   }
   cudaGraphDestroy(g);
   cudaStreamDestroy(cs);
@@ -424,6 +440,7 @@ dem_memory memory_of(long long N, long long S, long long C, const dem_options* o
   dem_memory m;
   m.per_particle = 3 * 24 + 2 * 8 + 5 * 4      /* pos vel angv, rad pmove, lqd lqd_old id plevel nidx */
                    + 3 * 24 + 8 + 3 * 4        /* tmp copies used while permuting */
+                   + 2 * 24                    /* staging of the force and moment exports */
                    + 2 * 24 + 8                /* force mom rmom */
                    + 4 + 12 + 4 + 4 + 12 + 4 + 4 /* num_nebor wlist nwall and their copies, nidx_old */
                    + 2 * 3 * 64                /* wall records and their copies */
@@ -525,6 +542,7 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   c->slots = s->n_pp_slots;
   c->mx = nullptr;
   c->graph_exec[0] = c->graph_exec[1] = nullptr;
+  c->graph_one[0] = c->graph_one[1] = nullptr;
   c->parity = 0;
   c->cap_w = nullptr;
   c->theta_max = 0.52359878f; /* 30 degrees */
@@ -559,6 +577,7 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   A(b.pos, N); A(b.vel, N); A(b.angv, N); A(b.rad, N); A(b.pmove, N); A(b.lqd, N); A(b.lqd_old, N);
   A(b.id, N); A(b.plevel, N); A(b.nidx, N);
   A(b.tmp_pos, N); A(b.tmp_vel, N); A(b.tmp_angv, N); A(b.tmp_rad, N); A(b.tmp_lqd, N); A(b.tmp_id, N);
+  A(b.tmp_out, 2 * N);
   A(b.tmp_plevel, N);
   A(b.force, N); A(b.mom, N); A(b.rmom, N);
   A(b.nebor, S); A(b.num_nebor, N); A(b.wlist, 3 * N); A(b.nwall, N);
@@ -676,7 +695,8 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
   if (!c || !pos) return fail(DEM_ERR_ARG, "dem_set_state: null argument");
   const size_t N = (size_t)c->n;
   EngineBufs& b = c->b;
-  /* host arrays (caller order) go to the tmp buffers, then a gather by id */
+  /* host arrays (caller order) go to the tmp buffers (copy engine), then a
+   * gather by id into cell order */
   cudaError_t e = cudaMemcpyAsync(b.tmp_pos, pos, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && vel) e = cudaMemcpyAsync(b.tmp_vel, vel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && angvel)
@@ -711,14 +731,23 @@ extern "C" dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, doub
     double3* host;
     const double3* dev;
   } items[5] = {{pos, b.pos}, {vel, b.vel}, {angvel, b.angv}, {force, b.force}, {mom, b.mom}};
+  /* caller order: each array gathered through the inverse of the cell order
+   * into its own staging buffer, then every copy to the host queued behind
+   * the gathers and one wait for all of them */
+  double3* stage[5] = {b.tmp_pos, b.tmp_vel, b.tmp_angv, b.tmp_out, b.tmp_out + N};
+  k_inverse<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_id);
+  int k = 0;
   for (auto& it : items) {
     if (!it.host) continue;
-    k_export<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, it.dev, b.tmp_pos);
-    cudaError_t e = cudaMemcpyAsync(it.host, b.tmp_pos, sizeof(double3) * N, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    k_export_gather<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.tmp_id, it.dev, stage[k++]);
+  }
+  k = 0;
+  for (auto& it : items) {
+    if (!it.host) continue;
+    cudaError_t e = cudaMemcpyAsync(it.host, stage[k++], sizeof(double3) * N, cudaMemcpyDeviceToHost, c->stream);
     if (e != cudaSuccess) return cuda_check(e, "dem_get_state");
   }
-  return DEM_OK;
+  return cuda_check(cudaStreamSynchronize(c->stream), "dem_get_state");
 }
 
 extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
@@ -731,7 +760,7 @@ extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
     while (left >= G) {
       const int p = mixed ? c->parity : 0;
       if (!c->graph_exec[p]) {
-        st = build_graph(c, G, p);
+        st = build_graph(c, G, p, &c->graph_exec[p]);
         if (st != DEM_OK) return st;
       }
       cudaError_t e = cudaGraphLaunch(c->graph_exec[p], c->stream);
@@ -741,6 +770,20 @@ extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
       c->ctime += G * c->s.sim.dt;
       if (mixed && (G & 1)) c->parity ^= 1;
     }
+  }
+  /* the remainder, one-step graphs (the rebuild decided on the device) */
+  while (c->opt.use_graph && left > 0) {
+    const int p = c->opt.precision == DEM_PREC_MIXED ? c->parity : 0;
+    if (!c->graph_one[p]) {
+      st = build_graph(c, 1, p, &c->graph_one[p]);
+      if (st != DEM_OK) return st;
+    }
+    cudaError_t e = cudaGraphLaunch(c->graph_one[p], c->stream);
+    if (e != cudaSuccess) return cuda_check(e, "cudaGraphLaunch");
+    left--;
+    c->iter++;
+    c->ctime += c->s.sim.dt;
+    if (c->opt.precision == DEM_PREC_MIXED) c->parity ^= 1;
   }
   while (left > 0) {
     st = host_step(c);

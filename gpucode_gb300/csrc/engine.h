@@ -35,6 +35,7 @@ struct EngineBufs {
   double *rad, *pmove;
   int *lqd, *lqd_old, *id, *plevel, *nidx;
   double3 *tmp_pos, *tmp_vel, *tmp_angv;
+  double3* tmp_out; /* 2 N: staging of exported arrays beside the three above */
   double* tmp_rad;
   int *tmp_lqd, *tmp_id, *tmp_plevel;
   double3 *force, *mom;
@@ -81,8 +82,10 @@ struct dem_ctx {
   long long rebuilds_host;
   double ctime;
   dem::MixedState* mx;
-  /* CUDA graphs of opt.graph_steps steps, one per starting shadow parity */
+  /* CUDA graphs of opt.graph_steps steps, one per starting shadow parity, and
+   * of one step (the remainder of a dem_step call) */
   cudaGraphExec_t graph_exec[2];
+  cudaGraphExec_t graph_one[2];
   int parity; /* mixed: which shadow buffer the next step reads */
   /* learned capillary closure (DEM_CAP_MLP): the staged network on the device
    * (NULL until dem_set_capnet) and the particles' contact angles */
