@@ -37,6 +37,7 @@ UNITS = [
     ("mixed.cu", ["-use_fast_math"]),
     ("capnet.cu", []),
     ("tune.cu", []),
+    ("feed.cu", []),
 ]
 
 

@@ -543,6 +543,7 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   c->mx = nullptr;
   c->graph_exec[0] = c->graph_exec[1] = nullptr;
   c->graph_one[0] = c->graph_one[1] = nullptr;
+  c->moving_walls = s->cyl.topv != 0.0 ? 1 : 0;
   c->parity = 0;
   c->cap_w = nullptr;
   c->theta_max = 0.52359878f; /* 30 degrees */
@@ -663,6 +664,9 @@ extern "C" dem_status dem_set_systems(dem_ctx* c, int n_sys, const int* system_o
   up(sw, w.data(), sizeof(int) * (size_t)n_sys);
   if (st != DEM_OK) return st;
   b.cyl = cyls;
+  c->moving_walls = 0;
+  for (int k = 0; k < n_sys; k++)
+    if (cyl[k].topv != 0.0) c->moving_walls = 1;
   b.sys_of_id = sys;
   b.sys_wet = sw;
   b.n_sys = n_sys;

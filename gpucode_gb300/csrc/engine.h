@@ -87,6 +87,7 @@ struct dem_ctx {
   cudaGraphExec_t graph_exec[2];
   cudaGraphExec_t graph_one[2];
   int parity; /* mixed: which shadow buffer the next step reads */
+  int moving_walls; /* a cylinder's top wall moves (topv != 0): moved before every step's wall contacts */
   /* learned capillary closure (DEM_CAP_MLP): the staged network on the device
    * (NULL until dem_set_capnet) and the particles' contact angles */
   void* cap_w;

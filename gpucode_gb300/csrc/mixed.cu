@@ -1125,6 +1125,12 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
                        twor * twor * twor, A.F, A.M, A.R, A.wet, (unsigned)nn, A.ncont, A.nbr, A.nmlp, A.nfall);
 }
 
+/* CirPWInterG's wall motion (kernel.cu:966-969): every cylinder's top wall
+ * moves by topv dt before any particle meets it this step */
+__global__ void k_move_walls(CylinderBC* cyl, int n_cyl, double dt) {
+  for (int k = threadIdx.x; k < n_cyl; k += blockDim.x) cyl[k].Tw = cyl[k].Tw + cyl[k].topv * dt;
+}
+
 __global__ void k_shadows(int n, const double3* __restrict__ pos, const double3* __restrict__ vel,
                           const double3* __restrict__ angv, const double* __restrict__ rad, const int* __restrict__ lqd,
                           double3 off, int bin_exp, float lo_scale, float4* __restrict__ phi, float4* __restrict__ plo,
@@ -1289,6 +1295,11 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;
   if (net && !c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
   const int g = grid_for(c->n, bs);
+  if (c->moving_walls) {
+    k_move_walls<<<1, 32, 0, s>>>(b.cyl, b.n_sys > 0 ? b.n_sys : 1, c->s.prm.dt);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_check(e, "mixed_step wall motion");
+  }
   const bool thread_loop = c->opt.pair_mode == DEM_PAIRS_THREAD || (c->opt.pair_mode == DEM_PAIRS_AUTO && net);
   if (thread_loop) {
     if (net) k_step_mixed<true, true><<<g, bs, kCapSmem, s>>>(a);

@@ -353,6 +353,18 @@ dem_status dem_load(dem_ctx* c, const char* path);
 /* Seed of ParticleFeed's generator (the reference seeds from the clock,
  * ParticleFeed.cpp:17; here feeds are reproducible). */
 void dem_set_feed_seed(unsigned long long seed);
+/* ParticleFeed (ParticleFeed.cpp:8-72) on the device arrays, replacing the
+ * sequence main.cpp:442-448 (positions down, ParticleFeed, positions up):
+ * dPos / dRad are device arrays of capacity NP (dRad holds every particle's
+ * radius, as hRad does); up to 60000 new particles numParticle.. are placed in
+ * the feed band with the reference's draws and clearance (r_i + r_j + 0.002),
+ * in parallel rounds, each given up after 500 tries; the batch keeps the
+ * particles below the first one that failed.  Counter-based generator: the
+ * same seed gives the same positions.  Allocates its scratch with cudaMalloc
+ * and synchronises the device.  Returns the new particle count, or -1
+ * (dem_last_error). */
+int ParticleFeedDevice(FeedZone* Feedcube, CylinderBC* h_Cir, double InitParSize, double3* dPos,
+                       double* dRad, int numParticle, int NP, unsigned long long seed);
 /* Reads and clears the error word of the reference-compatible entry points:
  * bit 1 = a neighbour list stopped at its level's slot capacity (the
  * reference would write past it, kernel.cu:833-836), bit 4 = a particle hashed

@@ -54,6 +54,27 @@ def test_mixed_engine_lockstep(cuda, make, pairs):
     eng.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_moving_top_wall_lockstep(cuda, precision):
+    """A lid descending onto the bed (CylinderBC.topv < 0; the reference moves
+    the top wall by topv dt every step, kernel.cu:966-969): the wall moves once
+    per step before any particle meets it, and forces, state, wall lists and
+    wall histories follow the oracle step by step while the lid presses into
+    the top layer."""
+    w = _workloads.small_dry()
+    pos, vel, ang = _workloads.stirred(w)
+    s = w.setup.s
+    top = float((pos[:, 2] + w.setup.rad).max())
+    s.cyl.Tw = top + 0.01
+    s.cyl.topv = -0.05 / (250 * s.prm.dt)  # 0.05 diameters over the run
+    eng = Engine(w.setup, precision=precision, use_graph=False)
+    tol, budget = (FP64_TOL, 0.0) if precision == "fp64" else (MIXED_TOL, 0.01)
+    worst = _lockstep.run(eng, w, pos, vel, ang, steps=250, tol=tol, mismatch_budget=budget)
+    assert worst["rebuilds"] >= 2, worst
+    assert eng.stats()["wall_contacts"] > 0
+    eng.close()
+
+
 @pytest.mark.parametrize("make", [_workloads.small_dry, _workloads.small_wet])
 def test_pair_loops_agree(cuda, make):
     """The warp-cooperative pair loop and the thread-per-particle one evaluate
