@@ -19,6 +19,7 @@
  *  - ParticleFeed draws from a seeded generator (dem_set_feed_seed) instead of
  *    srand(time(NULL)) (ParticleFeed.cpp:17), so feeds are reproducible.
  */
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -539,6 +540,70 @@ extern "C" void WrtTec(double3* hPos, double3* hVel, double3* hForce, double3* h
                  hPos[ip].x, hPos[ip].y, hPos[ip].z, hRad[ip], hVel[ip].x, hVel[ip].y, hVel[ip].z,
                  std::sqrt(w.x * w.x + w.y * w.y + w.z * w.z),
                  std::sqrt(F.x * F.x + F.y * F.y + F.z * F.z));
+  }
+  std::fclose(o);
+}
+
+/* ---------------------------------------------------------------------- */
+/* binary column output beside WrtTec                                       */
+/* ---------------------------------------------------------------------- */
+
+extern "C" void WrtBin(double3* hPos, double3* hVel, double3* hForce, double3* hAngVel, SIMULATION* h_dem,
+                       double* hRad, UNIT* Rdu, int TotalParticle, int NP) {
+  (void)NP;
+  /* WrtTec's quantities (WriteTec.cpp:28-35) at full precision, one column
+   * after the other: a file header on the first output (magic, column count,
+   * eight-byte column names), then per call a zone: tag, time [s], count and
+   * the nine columns of `count` doubles */
+  const char* filename = "particle_info.bin";
+  static const char names[9][8] = {"X", "Y", "Z", "R", "VX", "VY", "VZ", "W", "F"};
+  if (h_dem->Outs == 0) {
+    FILE* o = std::fopen(filename, "wb");
+    if (!o) return;
+    const char magic[8] = {'D', 'E', 'M', 'C', 'O', 'L', '0', '1'};
+    const int ncol = 9;
+    std::fwrite(magic, 1, 8, o);
+    std::fwrite(&ncol, sizeof(int), 1, o);
+    std::fwrite(names, 8, 9, o);
+    std::fclose(o);
+  }
+  FILE* o = std::fopen(filename, "ab");
+  if (!o) return;
+  const char tag[8] = {'Z', 'O', 'N', 'E', 0, 0, 0, 0};
+  const double t = h_dem->ctime * Rdu->rtunit;
+  const long long n = TotalParticle > 0 ? TotalParticle : 0;
+  std::fwrite(tag, 1, 8, o);
+  std::fwrite(&t, sizeof(double), 1, o);
+  std::fwrite(&n, sizeof(long long), 1, o);
+  std::vector<double> buf((size_t)std::min<long long>(n, 1 << 16));
+  for (int col = 0; col < 9; col++) {
+    for (long long i0 = 0; i0 < n; i0 += (long long)buf.size()) {
+      const long long m = std::min<long long>((long long)buf.size(), n - i0);
+      for (long long k = 0; k < m; k++) {
+        const long long ip = i0 + k;
+        double v;
+        switch (col) {
+          case 0: v = hPos[ip].x; break;
+          case 1: v = hPos[ip].y; break;
+          case 2: v = hPos[ip].z; break;
+          case 3: v = hRad[ip]; break;
+          case 4: v = hVel[ip].x; break;
+          case 5: v = hVel[ip].y; break;
+          case 6: v = hVel[ip].z; break;
+          case 7: {
+            const double3 w = hAngVel[ip];
+            v = std::sqrt(w.x * w.x + w.y * w.y + w.z * w.z);
+            break;
+          }
+          default: {
+            const double3 F = hForce[ip];
+            v = std::sqrt(F.x * F.x + F.y * F.y + F.z * F.z);
+          }
+        }
+        buf[(size_t)k] = v;
+      }
+      std::fwrite(buf.data(), sizeof(double), (size_t)m, o);
+    }
   }
   std::fclose(o);
 }

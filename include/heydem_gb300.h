@@ -123,6 +123,14 @@ void UnitReduce(UNIT* Rdu, CylinderBC* h_Cir, FeedZone* Feedcube, LOADMODE* h_lo
                 int RESTART, char* genfile);                                                       /* heydem.h:432 */
 int ParticleFeed(FeedZone* Feedcube, CylinderBC* h_Cir, double InitParSize, double3* hPos,
                  double* hRad, int numParticle, int NP);                                           /* heydem.h:440 */
+/* WrtTec's output (WriteTec.cpp:9-38) -- the same quantities X Y Z R VX VY VZ
+ * |w| |F| and zones -- as full-precision binary columns in particle_info.bin
+ * (no counterpart in the reference: at 10^7 particles the ASCII zone is
+ * ~1.5 GB of formatted text).  Layout: "DEMCOL01", int32 column count,
+ * 8-byte column names; per call "ZONE\0\0\0\0", float64 time [s], int64 count,
+ * then each column as count float64 values. */
+void WrtBin(double3* hPos, double3* hVel, double3* hForce, double3* hAngVel, SIMULATION* h_dem,
+            double* hRad, UNIT* Rdu, int TotalParticle, int NP);
 
 /* constant upload (kernel.cu:22-50) */
 void setMaterial(MatType* h_Mat);                                                                  /* heydem.h:453 */

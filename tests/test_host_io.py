@@ -168,6 +168,40 @@ def test_wrtec_matches_reference_byte_for_byte(in_tmp):
     assert outs["mine"] == outs["ref"]
 
 
+def test_binary_columns_hold_the_tecplot_quantities(in_tmp):
+    """WrtBin writes WrtTec's quantities and zones as full-precision columns:
+    every value agrees with the Tecplot text to its 5 printed decimals, and
+    the time of each zone to its 6"""
+    from gpucode_gb300.output import read_columns
+
+    lib = _abi.load()
+    rng = np.random.Generator(np.random.PCG64(9))
+    n = 1000
+    pos, vel, frc, ang = (rng.standard_normal((n, 3)) * 3 for _ in range(4))
+    rad = rng.uniform(0.2, 0.5, n)
+    sim = _abi.SIMULATION()
+    unit = _abi.UNIT()
+    unit.rtunit = 0.0123
+    P = _abi.ptr
+    for outs_i in (0, 1, 2):
+        sim.Outs = outs_i
+        sim.ctime = 1.5 + outs_i
+        lib.WrtTec(P(pos), P(vel), P(frc), P(ang), C.byref(sim), P(rad), C.byref(unit), n, n)
+        lib.WrtBin(P(pos), P(vel), P(frc), P(ang), C.byref(sim), P(rad), C.byref(unit), n, n)
+    names, zones = read_columns("particle_info.bin")
+    assert names == ["X", "Y", "Z", "R", "VX", "VY", "VZ", "W", "F"] and len(zones) == 3
+    text = open("particle_info.dat").read().splitlines()
+    rows = [ln for ln in text if ln and ln[0] in " -0123456789" and not ln.startswith("ZONE")]
+    tec = np.array([[float(x) for x in ln.split()] for ln in rows]).reshape(3, n, 9)
+    times = [float(ln.split('"')[1].split()[0]) for ln in text if ln.startswith("ZONE")]
+    for k, z in enumerate(zones):
+        assert z["n"] == n and abs(z["time"] - times[k]) <= 5e-7
+        cols = np.stack([z[c] for c in names], 1)
+        np.testing.assert_allclose(cols, tec[k], rtol=0, atol=5.01e-6)
+        np.testing.assert_array_equal(z["X"], pos[:, 0])
+        np.testing.assert_array_equal(z["W"], np.sqrt((ang * ang).sum(1)))
+
+
 def test_loadpara_reads_checkpoint_header(in_tmp):
     lib = _abi.load()
     open("heyi_dump.dat", "wb").write(b"SYSTEM Info\n1234 7 1200\n" + b"\x00\x01binary")
