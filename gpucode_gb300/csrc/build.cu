@@ -214,16 +214,18 @@ __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* _
         if (s.x < 0) s.x = 0;
         if (e.x > gs.x - 1) e.x = gs.x - 1;
         if (s.y < 0 || s.z < 0 || s.y > gs.y - 1 || s.z > gs.z - 1) continue;
-        while (s.x != e.x) {
-          if (cell_start[grid_hash(s, iL, lv) + cell_sum] == -1) s.x++;
-          else break;
+        /* the row's particles: from the start of its first non-empty cell to
+         * the end of its last one (cells of a row are consecutive in sorted
+         * order).  The reference walks in from both ends one dependent load
+         * at a time (kernel.cu:775-790); every cell's range is read here
+         * with independent loads -- the same range, the same append order. */
+        int first = -1, last = -1;
+        const int row = grid_hash(s, iL, lv) + cell_sum;
+        for (int x = 0; x <= e.x - s.x; x++) {
+          const int cs = __ldg(cell_start + row + x), ce = __ldg(cell_end + row + x);
+          if (first == -1) first = cs;
+          if (ce != -1) last = ce;
         }
-        const int first = cell_start[grid_hash(s, iL, lv) + cell_sum];
-        while (s.x != e.x) {
-          if (cell_end[grid_hash(e, iL, lv) + cell_sum] == -1) e.x--;
-          else break;
-        }
-        const int last = cell_end[grid_hash(e, iL, lv) + cell_sum];
         if (first == -1 || last == -1) continue;
         for (int q = first; q < last; q++) {
           const int j = sorted_src ? sorted_src[q] : q;
