@@ -83,6 +83,8 @@ struct MixArgs {
   const CylinderBC* cyl;
   int n, force_cap;
   double3 off;
+  float3 offf;    /* the offset rounded to FP32 */
+  float wall_tol; /* bound on the error of the FP32 wall gap from the shadow */
   int bin_exp;
   float lo_scale;
   double dt, move_limit; /* 0.3 * SearchGap */
@@ -402,10 +404,28 @@ __device__ __forceinline__ void finish_particle(const MixArgs& a, int q, int qq,
     double3 jvel = make_double3(0.0, 0.0, 0.0);
     for (int w = 0; w < nw; w++) {
       const int kind = a.wlist[3 * qq + w];
+      /* the top wall's velocity carries over to the walls after it in the
+       * list, as the reference's jVel does (kernel.cu:987-1020) */
+      if (kind == 0) jvel = make_double3(0.0, 0.0, cy.topv);
+      /* A wall the particle certainly does not touch costs no FP64 work:
+       * a coarse gap from the shadow (hi part of x + offset, truncated to
+       * the binade) is within wall_tol of the exact one -- 5 binade ulps for
+       * the flat walls, 11 for the curved one, bounded by 16 -- so only
+       * particles within wall_tol of a wall take the reference's geometry. */
+      float gc;
+      if (kind == 0 || kind == 1) {
+        gc = fabsf(hi.z - (d2f(kind == 0 ? cy.Tw : cy.Bw) + a.offf.z)) - ri;
+      } else if (kind == 2) {
+        const float cxo = d2f(cy.cir.x) + a.offf.x, cyo = d2f(cy.cir.y) + a.offf.y;
+        const float dx = hi.x - cxo, dy = hi.y - cyo;
+        gc = fabsf(sqrtf(dx * dx + dy * dy) - d2f(cy.R)) - ri;
+      } else {
+        continue;
+      }
+      if (gc > a.wall_tol) continue;
       double3 jp;
       if (kind == 0) {
         jp = make_double3(p.x, p.y, cy.Tw);
-        jvel = make_double3(0.0, 0.0, cy.topv);
       } else if (kind == 1) {
         jp = make_double3(p.x, p.y, cy.Bw);
       } else if (kind == 2) {
@@ -1270,6 +1290,8 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   a.n = c->n;
   a.force_cap = c->s.force_cap;
   a.off = m->off;
+  a.offf = make_float3((float)m->off.x, (float)m->off.y, (float)m->off.z);
+  a.wall_tol = 4.0f * m->coarse_tol; /* 16 binade ulps */
   a.bin_exp = m->bin_exp;
   a.lo_scale = m->lo_scale;
   a.dt = c->s.prm.dt;
