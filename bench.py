@@ -103,6 +103,27 @@ def _dist():
     return ws, rank
 
 
+def slowest(local: float, ws: int, device: str = "cuda") -> float:
+    """the largest of every rank's value (a time): the job is as fast as its
+    slowest replica"""
+    if ws <= 1:
+        return local
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([local], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(local_s: float, particles: int, steps: int, ws: int, device: str = "cuda") -> tuple[float, float]:
+    """whole-job particle-steps/s of `ws` independent replicas, each stepping
+    `particles` particles `steps` times: all ranks' particle-steps over the
+    slowest rank's time; -> (rate, slowest time [s])"""
+    t = slowest(local_s, ws, device)
+    return ws * particles * steps / t, t
+
+
 def cpu_oracle_rate(w, pos, steps: int, threads: int) -> tuple[float, str]:
     """The FP64 oracle (reference algorithm on the host cores, OpenMP) on the same bed."""
     os.environ["OMP_NUM_THREADS"] = str(threads)
@@ -679,12 +700,9 @@ def main():
     ms, t_wall, ck, s0, s1 = timed_steps(eng, args.steps)
     steps_run = args.settle + args.warmup + args.steps
     pos_mixed = eng.get_state()["pos"]
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     steps = args.steps
-    value = ws * n * steps / (ms / 1000.0)
+    value, t_slow = replica_rate(ms / 1000.0, n, steps, ws)
+    ms = 1000.0 * t_slow
 
     # measured pair counts per particle-step over the timed region
     d = {k: s1[k] - s0[k] for k in ("nb_entries", "contacts", "bridges", "wall_contacts", "rebuilds")}
@@ -715,11 +733,7 @@ def main():
         check(eng.lib.dem_step(eng.h, 1), "dem_step")
         check(eng.lib.dem_get_state(eng.h, ptr(hp), ptr(hv), ptr(hw), ptr(hf), None), "dem_get_state")
     e2e_t = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_t], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(t.item())
-    e2e = ws * n * E / e2e_t
+    e2e, e2e_t = replica_rate(e2e_t, n, E, ws)
     eng.sync()
 
     # accuracy: the same bed, the same number of steps, all-FP64 reference formulas
