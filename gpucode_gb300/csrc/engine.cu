@@ -231,12 +231,6 @@ __global__ void k_export_gather(int n, const int* __restrict__ inv, const double
   if (i < n) dst[i] = src[inv[i]];
 }
 
-__global__ void k_export(int n, const int* __restrict__ id, const double3* __restrict__ src, double3* __restrict__ dst) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  dst[id[q]] = src[q];
-}
-
 __global__ void k_check_finite(int n, const double3* __restrict__ pos, const double3* __restrict__ vel,
                                int* __restrict__ err) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;

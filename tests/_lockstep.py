@@ -58,9 +58,15 @@ def slip_ties(sim, w, num, hist, rel: float = 1e-9) -> np.ndarray:
     re-derived here from each contact's stored overlap and plastic state."""
     s = w.setup.s
     cal = s.cal
+    out = np.zeros(w.setup.n)
     ii, kk, _ = sim.slots_of(num)
-    if len(ii) == 0:
-        return np.zeros(w.setup.n)
+    if len(ii):
+        _pair_ties(sim, w, cal, ii, hist, rel, out)
+    _wall_ties(sim, w, s, rel, out)
+    return out
+
+
+def _pair_ties(sim, w, cal, ii, hist, rel, out) -> None:
     _, lists = sim.lists()
     jj = np.concatenate([lists[i] for i in range(w.setup.n)]).astype(np.int64)
     ri, rj = w.setup.rad[ii], w.setup.rad[jj]
@@ -77,8 +83,10 @@ def slip_ties(sim, w, num, hist, rel: float = 1e-9) -> np.ndarray:
                                       np.sqrt(np.abs(R * nrm)))
         dlen = np.linalg.norm(hist[:, 0:3], axis=1)
         tie = (dsmx > 0) & (np.abs(dlen - dsmx) <= rel * dsmx)
-    out = np.zeros(w.setup.n)
     np.add.at(out, ii[tie], 2.0 * cal.sfrc * fN[tie])
+
+
+def _wall_ties(sim, w, s, rel, out) -> None:
     # wall contacts: R* = r_i, the wall constants, the same slip test (kernel.cu:321)
     pw = s.pwcal
     nw = sim.arr("nwall", np.int32, w.setup.n)
@@ -102,7 +110,6 @@ def slip_ties(sim, w, num, hist, rel: float = 1e-9) -> np.ndarray:
             t = (dsmx > 0) & (np.abs(dlen - dsmx) <= rel * dsmx)
         idx = np.flatnonzero(m)
         np.add.at(out, idx[t], 2.0 * pw.sfrc * fN[t])
-    return out
 
 
 def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: float = 0.0) -> dict:

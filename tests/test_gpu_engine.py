@@ -182,3 +182,44 @@ def test_nonfinite_state_is_reported(cuda):
     with pytest.raises(_abi.DemError) as ei:
         e.sync()
     assert ei.value.code == _abi.DEM_ERR_NONFINITE
+
+
+@pytest.mark.parametrize("n", [1, 2, 37])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tiny_and_ragged_beds_lockstep(cuda, n, precision):
+    """A single sphere (no neighbours: the floor and the side wall only), a
+    pair, and a bed that fills neither a warp nor a block: the pair loops'
+    partial warps and empty lists follow the oracle step by step."""
+    w = _workloads.small_dry(n=n, seed=5)
+    pos, vel, ang = _workloads.stirred(w, vscale=2.0)
+    eng = Engine(w.setup, precision=precision, use_graph=False)
+    tol, budget = (FP64_TOL, 0.0) if precision == "fp64" else (MIXED_TOL, 0.01)
+    worst = _lockstep.run(eng, w, pos, vel, ang, steps=120, tol=tol, mismatch_budget=budget)
+    assert worst["rebuilds"] >= 1, worst
+    eng.close()
+
+
+def test_empty_setup_is_rejected():
+    """no particles: dem_create refuses the set-up instead of launching empty grids"""
+    w = _workloads.small_dry(n=8)
+    w.setup.s.np = 0
+    with pytest.raises(_abi.DemError) as ei:
+        Engine(w.setup, precision="mixed")
+    assert ei.value.code == _abi.DEM_ERR_ARG
+
+
+def test_particle_outside_the_grid_is_reported(cuda):
+    """a particle far outside the domain hashes past the last cell: the build
+    keeps it in the last cell instead of writing past the cell arrays (the
+    reference clamps to the grid size, kernel.cu:627-629, one past the end)
+    and dem_sync reports DEM_ERR_CELL"""
+    w = _workloads.small_dry()
+    pos, vel, ang = _workloads.stirred(w)
+    pos[7, 2] = 1.0e4
+    e = Engine(w.setup, precision="mixed")
+    e.set_state(pos, vel, ang)
+    e.step(1)
+    with pytest.raises(_abi.DemError) as ei:
+        e.sync()
+    assert ei.value.code == _abi.DEM_ERR_CELL
+    e.close()
