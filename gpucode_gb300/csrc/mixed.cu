@@ -1059,6 +1059,10 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
           const PairGeo g = coop_geo<WET>(a, ow, o, (wetm >> o) & 1u, s, j, hj);
           geo[p - c0] = g;
           meta = g.meta;
+          if (meta & kGContact) { /* phase B will need them: start bringing them in */
+            prefetch_l2(a.rec + s);
+            prefetch_l2(a.w_in + j);
+          }
         }
         const unsigned mc = __ballot_sync(FULL, meta & kGContact);
         const unsigned mb = __ballot_sync(FULL, meta & kGBridge);
