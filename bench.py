@@ -500,6 +500,10 @@ def run_wet_large(args, which: str):
              "roofline": {"kernel": step_kernel("auto", cap), "kernel_ms": ms_k.value, "bytes_per_particle": bpp,
                           "achieved": ach, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                           "frac": ach / peak, "l2": "working set far above L2 (no eviction needed)"}}
+        if cap == "formula":
+            r["kernels"] = kernel_table(e, n)
+            r["kernels_note"] = ("one step with a forced rebuild timed kernel by kernel (CUDA events); DRAM bytes "
+                                 "scaled from the 200,000-sphere ncu capture by particle count")
         if cap == "mlp":
             r["network_evaluations_per_step"] = (s1["cap_mlp"] - s0["cap_mlp"]) / (steps - 16)
             r["formula_fallback_fraction"] = (s1["cap_fallback"] - s0["cap_fallback"]) / max(
@@ -533,6 +537,43 @@ def run_wet_large(args, which: str):
         "closure_training": {"samples": used, "epochs": rep["epochs"], "fit_seconds": rep["seconds"],
                              "bed": "200,000-sphere wet bed while settling"},
         "memory_plan": fit, "runs": out, "sub_cylinder_vs_fp64": sub}), flush=True)
+
+
+CELL_SORT = ("k_hash_count", "k_tile_sums", "k_scan_tiles", "k_cell_ranges", "k_scatter", "k_cell_order")
+
+
+def kernel_bytes_per_particle() -> dict:
+    """DRAM bytes per particle of each kernel of a rebuild + step, from the
+    committed ncu table of the 200,000-sphere bed (MB per launch / 200,000);
+    the cell sort's launches summed under the group name the library reports"""
+    p = ROOT / "profiles" / "launches_wet200k.md"
+    out = {}
+    if not p.exists():
+        return out
+    for line in p.read_text().splitlines():
+        f = [x.strip() for x in line.strip().strip("|").split("|")]
+        if len(f) == 6 and f[0].startswith("k_") and f[2].replace(".", "").isdigit():
+            try:
+                out[f[0]] = float(f[3]) * 1e6 / 200_000
+            except ValueError:
+                pass
+    out["cell sort (k_hash_count .. k_cell_order)"] = sum(out.get(k, 0.0) for k in CELL_SORT)
+    return out
+
+
+def kernel_table(e, n: int) -> list:
+    """one rebuild + step of engine e timed kernel by kernel, with achieved GB/s
+    from the 200k bed's measured bytes per particle scaled to n particles"""
+    bpp = kernel_bytes_per_particle()
+    peak, _ = _peaks()
+    rows = []
+    for name, ms in e.profile_kernels():
+        key = "k_step_coop<1,0>" if name == "step kernel" else name
+        b = bpp.get(key)
+        gbs = None if (b is None or ms <= 0) else b * n / (ms * 1e-3) / 1e9
+        rows.append({"kernel": name, "ms": ms, "dram_bytes_scaled": None if b is None else b * n,
+                     "achieved_gbs": gbs, "frac": None if gbs is None else gbs / peak})
+    return rows
 
 
 def step_kernel(pairs: str, capillary: str = "formula") -> str:
@@ -869,6 +910,7 @@ def main():
                          "bytes_per_particle": bytes_per_particle, "kernel_ms": ms_k.value},
             "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": cpu_sample},
+            "contact_evaluations_per_s": value * n_c,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * 72, "d2h_bytes_per_step": n * 96},
             "gpu_launches": launches_per_step * steps + rebuild_launches * d["rebuilds"],
             "clocks": ck,

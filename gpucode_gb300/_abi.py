@@ -150,6 +150,10 @@ class DemTuneResult(C.Structure):
                 ("n_tried", C.c_int), ("best_rate", C.c_double), ("rate", C.c_double * 64)]
 
 
+class DemKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 48), ("ms", C.c_double)]
+
+
 class CapnetFitOpts(C.Structure):
     _fields_ = [("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_float), ("val_frac", C.c_float),
                 ("seed", C.c_ulonglong)]
@@ -232,6 +236,7 @@ def _declare(lib: C.CDLL) -> None:
         "dem_l2_flush": (I, [P, P, C.c_size_t]),
         "dem_compat_errors": (I, []),
         "dem_set_systems": (I, [P, I, P, P, P]),
+        "dem_profile_kernels": (I, [P, P, I, C.POINTER(I)]),
         "dem_scale_cells": (I, [C.POINTER(DemSetup), C.c_double]),
         "dem_autotune": (I, [C.POINTER(DemInput), P, P, P, C.POINTER(DemOptions), C.POINTER(DemTuneSpace), I, P, P, P,
                              C.POINTER(DemSetup), C.POINTER(DemOptions), C.POINTER(DemTuneResult)]),

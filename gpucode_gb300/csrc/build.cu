@@ -278,7 +278,12 @@ __global__ void k_wall_list(const double3* __restrict__ pos, const double* __res
   int m = 0;
   if (p.z >= (c.Tw - (2.0 * r + search_gap))) row[m++] = 0;
   if (p.z <= ((2.0 * r + search_gap) + c.Bw)) row[m++] = 1;
-  const double dist = pow(pow((c.cir.x - p.x), 2.0) + pow((c.cir.y - p.y), 2.0), 0.5);
+  /* the reference writes pow(pow(dx, 2) + pow(dy, 2), 0.5): squares and a
+   * square root, correctly rounded (glibc's pow returns exactly these values,
+   * and this file is built without FMA contraction), at the cost of one
+   * FP64 square root instead of three FP64 pow calls */
+  const double dx = c.cir.x - p.x, dy = c.cir.y - p.y;
+  const double dist = sqrt(dx * dx + dy * dy);
   if (dist >= c.R - (2.0 * r + search_gap)) row[m++] = 2;
   nwall[i] = m;
 }

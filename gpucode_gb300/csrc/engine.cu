@@ -245,6 +245,15 @@ __global__ void k_check_finite(int n, const double3* __restrict__ pos, const dou
 HistAoS hist_pp(dem_ctx* c) { return HistAoS{c->b.rec, c->b.brg}; }
 HistAoS hist_pw(dem_ctx* c) { return HistAoS{c->b.wrec, nullptr}; }
 
+/* dem_profile_kernels: an event after the kernel(s) just enqueued */
+void mark(dem_ctx* c, cudaStream_t s, const char* name) {
+  if (!c->marks) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, s);
+  c->marks->emplace_back(name, e);
+}
+
 /* The whole rebuild, enqueued on s (graph-capturable: fixed pointers, no host sync). */
 dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
   EngineBufs& b = c->b;
@@ -254,18 +263,22 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
   if (c->opt.precision == DEM_PREC_MIXED) {
     st = mixed_pre_rebuild(c, parity, s);
     if (st != DEM_OK) return st;
+    mark(c, s, "k_lqd_from_shadow");
   }
   k_copy_old<<<grid_for(n, 128), 128, 0, s>>>(b.nebor, b.num_nebor, b.nidx, b.plevel, b.npars, b.nneb, b.rec, b.brg,
                                                b.wlist, b.nwall, b.wrec, b.nebor_old, b.num_nebor_old, b.nidx_old,
                                                b.rec_old, b.brg_old, b.wlist_old, b.nwall_old, b.wrec_old, n,
                                                b.counters);
+  mark(c, s, "k_copy_old");
   st = cell_sort(b.pos, b.plevel, reorder ? b.id : nullptr, n, c->lv, c->k, c->s.sys_ncells, b.sorted_hash,
                  b.sorted_src, b.cell_start, b.cell_end, b.scratch, b.err, s);
   if (st != DEM_OK) return st;
+  mark(c, s, "cell sort (k_hash_count .. k_cell_order)");
   if (reorder) {
     k_permute<<<grid_for(n, 256), 256, 0, s>>>(b.sorted_src, n, b.pos, b.vel, b.angv, b.rad, b.lqd, b.id, b.plevel,
                                                 b.tmp_pos, b.tmp_vel, b.tmp_angv, b.tmp_rad, b.tmp_lqd, b.tmp_id,
                                                 b.tmp_plevel, b.old_to_new);
+    mark(c, s, "k_permute");
     LevelStart ls;
     for (int l = 0; l < DEM_MAX_LEVELS; l++) {
       ls.v[l] = l < c->s.n_levels ? c->lstart[l] : 0;
@@ -274,6 +287,7 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
     k_copy_back<<<grid_for(n, 256), 256, 0, s>>>(n, b.tmp_pos, b.tmp_vel, b.tmp_angv, b.tmp_rad, b.tmp_lqd, b.tmp_id,
                                                   b.tmp_plevel, b.pos, b.vel, b.angv, b.rad, b.lqd, b.id, b.plevel,
                                                   b.nidx, b.pmove, ls, b.err);
+    mark(c, s, "k_copy_back");
   } else {
     cudaError_t e = cudaMemsetAsync(b.pmove, 0, sizeof(double) * (size_t)n, s);
     if (e != cudaSuccess) return cuda_check(e, "pmove reset");
@@ -284,16 +298,20 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
     st = mixed_shadows(c, parity, s);
     if (st != DEM_OK) return st;
     pre = mixed_prefilter(c, parity);
+    mark(c, s, "k_shadows");
   }
   st = neighbor_find(b.pos, b.rad, reorder ? nullptr : b.sorted_src, b.cell_start, b.cell_end, b.plevel, b.nidx,
                      c->lv, c->k, b.nebor, b.num_nebor, n, b.err, s, pre);
   if (st != DEM_OK) return st;
+  mark(c, s, "k_neighbor_find");
   st = wall_list(b.pos, b.rad, b.cyl, b.wlist, 3 * sizeof(int), b.nwall, n, c->k, s, b.id, b.sys_of_id);
   if (st != DEM_OK) return st;
+  mark(c, s, "k_wall_list");
   k_carry<<<grid_for(n, 128), 128, 0, s>>>(b.nebor, b.num_nebor, b.nidx, b.plevel, b.npars, b.nneb, b.nebor_old,
                                            b.num_nebor_old, b.nidx_old, b.rec_old, b.brg_old, b.rec, b.brg, b.wlist,
                                            b.nwall, b.wlist_old, b.nwall_old, b.wrec_old, b.wrec,
                                            reorder ? b.sorted_src : nullptr, reorder ? b.old_to_new : nullptr, n);
+  mark(c, s, "k_carry");
   return cuda_check(cudaGetLastError(), "rebuild launch");
 }
 
@@ -538,6 +556,7 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   c->graph_exec[0] = c->graph_exec[1] = nullptr;
   c->graph_one[0] = c->graph_one[1] = nullptr;
   c->moving_walls = s->cyl.topv != 0.0 ? 1 : 0;
+  c->marks = nullptr;
   c->parity = 0;
   c->cap_w = nullptr;
   c->theta_max = 0.52359878f; /* 30 degrees */
@@ -854,6 +873,45 @@ extern "C" dem_status dem_profile_step(dem_ctx* c, int reps, void* flush_buf, si
   cudaEventDestroy(e1);
   if (st == DEM_OK) *ms_avg = total / reps;
   return st;
+}
+
+extern "C" dem_status dem_profile_kernels(dem_ctx* c, dem_kernel_time* out, int max_out, int* n_out) {
+  if (!c || !out || max_out <= 0 || !n_out) return fail(DEM_ERR_ARG, "dem_profile_kernels: bad argument");
+  std::vector<std::pair<const char*, cudaEvent_t>> marks;
+  cudaEvent_t e0;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e != cudaSuccess) return cuda_check(e, "dem_profile_kernels");
+  /* one host-launched step with a forced rebuild, an event after each kernel */
+  e = cudaMemsetAsync(c->b.flag, 0, sizeof(int), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->b.need, 0, sizeof(int), c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+  dem_status st = cuda_check(e, "dem_profile_kernels");
+  c->marks = &marks;
+  if (st == DEM_OK) st = enqueue_rebuild(c, c->stream, c->parity);
+  if (st == DEM_OK) st = enqueue_step(c, c->stream, c->parity);
+  if (st == DEM_OK) mark(c, c->stream, c->opt.precision == DEM_PREC_MIXED ? "step kernel" : "FP64 step kernels");
+  c->marks = nullptr;
+  if (st == DEM_OK) st = cuda_check(cudaStreamSynchronize(c->stream), "dem_profile_kernels sync");
+  int k = 0;
+  cudaEvent_t prev = e0;
+  for (auto& m : marks) {
+    float ms = 0.f;
+    if (st == DEM_OK && k < max_out && cudaEventElapsedTime(&ms, prev, m.second) == cudaSuccess) {
+      std::memset(out[k].name, 0, sizeof(out[k].name));
+      std::strncpy(out[k].name, m.first, sizeof(out[k].name) - 1);
+      out[k].ms = ms;
+      k++;
+    }
+    prev = m.second;
+  }
+  for (auto& m : marks) cudaEventDestroy(m.second);
+  cudaEventDestroy(e0);
+  if (st != DEM_OK) return st;
+  *n_out = k;
+  if (c->opt.precision == DEM_PREC_MIXED) c->parity ^= 1;
+  c->iter++;
+  c->ctime += c->s.sim.dt;
+  return DEM_OK;
 }
 
 extern "C" dem_status dem_sync(dem_ctx* c) {

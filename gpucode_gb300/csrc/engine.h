@@ -21,6 +21,7 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
 #include <vector>
 
 #include "dem_internal.h"
@@ -88,6 +89,9 @@ struct dem_ctx {
   cudaGraphExec_t graph_one[2];
   int parity; /* mixed: which shadow buffer the next step reads */
   int moving_walls; /* a cylinder's top wall moves (topv != 0): moved before every step's wall contacts */
+  /* dem_profile_kernels: when set, the rebuild and the step record an event
+   * after each of their kernels (NULL otherwise, and always during capture) */
+  std::vector<std::pair<const char*, cudaEvent_t>>* marks;
   /* learned capillary closure (DEM_CAP_MLP): the staged network on the device
    * (NULL until dem_set_capnet) and the particles' contact angles */
   void* cap_w;

@@ -180,6 +180,14 @@ class Engine:
         check(self.lib.dem_set_systems(self.h, len(cylinders), ptr(sysv), C.cast(arr, C.c_void_p),
                                        None if w is None else ptr(w)), "dem_set_systems")
 
+    def profile_kernels(self) -> list[tuple[str, float]]:
+        """one step with a forced rebuild, timed kernel by kernel (dem_profile_kernels):
+        [(kernel, device ms)] in launch order"""
+        out = (_abi.DemKernelTime * 32)()
+        n = C.c_int()
+        check(self.lib.dem_profile_kernels(self.h, C.cast(out, C.c_void_p), 32, C.byref(n)), "dem_profile_kernels")
+        return [(out[k].name.decode(), out[k].ms) for k in range(n.value)]
+
     def save(self, path: str | os.PathLike, nbatch: int = 1) -> None:
         check(self.lib.dem_save(self.h, str(path).encode(), nbatch), "dem_save")
 

@@ -355,6 +355,11 @@ dem_status dem_set_systems(dem_ctx* c, int n_sys, const int* system_of_particle,
                            const int* wet);
 /* Write / read the full engine state (binary, with the reference's
  * "SYSTEM Info" text header so LoadPara can parse it). */
+/* One step with a forced neighbour rebuild, launched from the host with a CUDA
+ * event after each kernel: out[k] = {kernel (or group), device ms} in launch
+ * order, *n_out entries (at most max_out).  The step counts as a step. */
+typedef struct dem_kernel_time { char name[48]; double ms; } dem_kernel_time;
+dem_status dem_profile_kernels(dem_ctx* c, dem_kernel_time* out, int max_out, int* n_out);
 dem_status dem_save(dem_ctx* c, const char* path, int nBatch);
 dem_status dem_load(dem_ctx* c, const char* path);
 

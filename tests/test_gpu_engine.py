@@ -223,3 +223,27 @@ def test_particle_outside_the_grid_is_reported(cuda):
         e.sync()
     assert ei.value.code == _abi.DEM_ERR_CELL
     e.close()
+
+
+def test_profile_kernels_times_a_rebuild_and_a_step(cuda):
+    """dem_profile_kernels: one step with a forced rebuild, an event after each
+    kernel; it counts as a step and stepping goes on from it"""
+    w = _workloads.small_wet()
+    pos, vel, ang = _workloads.stirred(w)
+    e = Engine(w.setup, precision="mixed")
+    e.set_state(pos, vel, ang)
+    e.step(2)
+    e.sync()
+    s0 = e.stats()
+    rows = e.profile_kernels()
+    names = [r[0] for r in rows]
+    for k in ("k_copy_old", "k_permute", "k_neighbor_find", "k_wall_list", "k_carry"):
+        assert k in names, names
+    assert names[-1] == "step kernel"
+    assert all(ms >= 0.0 for _, ms in rows) and sum(ms for _, ms in rows) > 0.0
+    s1 = e.stats()
+    assert s1["iter"] == s0["iter"] + 1 and s1["rebuilds"] == s0["rebuilds"] + 1
+    e.step(5)
+    e.sync()
+    assert e.stats()["iter"] == s1["iter"] + 5
+    e.close()
