@@ -135,6 +135,36 @@ __device__ __forceinline__ float two_sum(float a, float b, float& err) {
   return s;
 }
 
+/* The overlap of spheres i and j from their shadows, exactly enough for a
+ * contact law: with a = hi_i - hi_j (exact: both in one binade) and
+ * b = lo_i - lo_j, d^2 - S^2 is accumulated from error-free pieces (FMA
+ * two-products, Knuth two-sums) and the overlap is (d^2 - S^2) / (d + S), so
+ * it keeps ~1e-7 relative accuracy although d and S agree to ~1e-4.  Returns
+ * the gap (negative: overlap); u is the unit vector from j to i, rj j's radius. */
+__device__ __forceinline__ float exact_gap(float4 hi, float4 lo, float4 hj, float4 lj, float ax, float ay, float az,
+                                           float3& u, float& rj) {
+  rj = hj.w + lj.w;
+  const float bx = lo.x - lj.x, by = lo.y - lj.y, bz = lo.z - lj.z;
+  const float px = ax * ax, py = ay * ay, pz = az * az;
+  const float ex = fmaf(ax, ax, -px), ey = fmaf(ay, ay, -py), ez = fmaf(az, az, -pz);
+  float t1, t2, es;
+  const float s1 = two_sum(px, py, t1);
+  const float s2 = two_sum(s1, pz, t2);
+  const float slo = (lo.w + lj.w);
+  const float Sh = two_sum(hi.w, hj.w, es);
+  const float Sl = es + slo;
+  const float qq2 = Sh * Sh, eq = fmaf(Sh, Sh, -qq2);
+  const float s3 = s2 - qq2;
+  const float small = (t1 + t2) + (ex + ey + ez - eq) + 2.0f * (ax * bx + ay * by + az * bz) -
+                      2.0f * Sh * Sl + (bx * bx + by * by + bz * bz) - Sl * Sl;
+  const float D = s3 + small;
+  const float dx = ax + bx, dy = ay + by, dz = az + bz;
+  const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float inv = __frcp_rn(dist);
+  u = make_float3(dx * inv, dy * inv, dz * inv);
+  return __fdividef(D, dist + (Sh + Sl));
+}
+
 /* ---- FP32 <-> FP64 through the integer pipe ----
  * On GB300 FP64 conversions issue on the scarce FP64 pipe; these move the bits
  * with integer operations instead.  d2f truncates the mantissa (error below one
@@ -276,6 +306,20 @@ __device__ __forceinline__ void store_rec(ContactRec* p, const MixedRec& r) {
   q[1] = o[1];
   q[2] = o[2];
   q[3] = o[3];
+}
+
+/* One p-p contact (gap < 0, unit vector u from j to i): relative velocity at
+ * the contact point, the law, and the 64-byte history record of slot s read
+ * and written back */
+__device__ __forceinline__ void pp_contact(const Law32& law, ContactRec* rec, float ri, float rj, float3 iv,
+                                           float3 iw, float4 vj4, float4 wj4, float3 u, float gap, float rfrc,
+                                           float dt, float3& dF, float3& dM, float& dR) {
+  MixedRec rc = load_rec(rec);
+  const float3 cpv = f3(iv.x - vj4.x, iv.y - vj4.y, iv.z - vj4.z) -
+                     crossf(iw * ri + f3(wj4.x, wj4.y, wj4.z) * rj, u);
+  const float ijRad = ri * rj / (ri + rj);
+  law32(law, ijRad, -gap, u, cpv, rc, ri, rfrc, dt, dF, dM, dR);
+  store_rec(rec, rc);
 }
 
 /* hi/lo split of a coordinate already shifted into the binade [2^k, 2^(k+1)):
@@ -602,39 +646,12 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
     float4 vj4 = make_float4(0.f, 0.f, 0.f, 0.f);
     if (WET) vj4 = ro(a.v_in + j);
     if (cand) {
-      const float4 lj = ro(a.plo_in + j);
-      rj = hj.w + lj.w;
-      const float bx = lo.x - lj.x, by = lo.y - lj.y, bz = lo.z - lj.z;
-      /* d^2 - S^2 from exact pieces */
-      const float px = ax * ax, py = ay * ay, pz = az * az;
-      const float ex = fmaf(ax, ax, -px), ey = fmaf(ay, ay, -py), ez = fmaf(az, az, -pz);
-      float t1, t2, es;
-      const float s1 = two_sum(px, py, t1);
-      const float s2 = two_sum(s1, pz, t2);
-      const float slo = (lo.w + lj.w);
-      const float Sh = two_sum(hi.w, hj.w, es);
-      const float Sl = es + slo;
-      const float qq2 = Sh * Sh, eq = fmaf(Sh, Sh, -qq2);
-      const float s3 = s2 - qq2;
-      const float small = (t1 + t2) + (ex + ey + ez - eq) + 2.0f * (ax * bx + ay * by + az * bz) -
-                          2.0f * Sh * Sl + (bx * bx + by * by + bz * bz) - Sl * Sl;
-      const float D = s3 + small;
-      const float dx = ax + bx, dy = ay + by, dz = az + bz;
-      const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
-      gap = __fdividef(D, dist + (Sh + Sl));
-      const float inv = __frcp_rn(dist);
-      u = f3(dx * inv, dy * inv, dz * inv);
+      gap = exact_gap(hi, lo, hj, ro(a.plo_in + j), ax, ay, az, u, rj);
       if (gap < 0.f) {
         if (!WET) vj4 = ro(a.v_in + j);
-        const float4 wj4 = ro(a.w_in + j);
-        const float3 jv = f3(vj4.x, vj4.y, vj4.z), jw = f3(wj4.x, wj4.y, wj4.z);
-        const float3 cpv = (iv - jv) - crossf(iw * ri + jw * rj, u);
-        const float ijRad = ri * rj / (ri + rj);
-        MixedRec rc = load_rec(a.rec + s);
         float3 dF, dM;
         float dR;
-        law32(a.pp, ijRad, -gap, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
-        store_rec(a.rec + s, rc);
+        pp_contact(a.pp, a.rec + s, ri, rj, iv, iw, vj4, ro(a.w_in + j), u, gap, a.rfrc, a.dtf, dF, dM, dR);
         F.add(dF);
         M.add(dM);
         R.add(dR);
@@ -822,30 +839,11 @@ __device__ __forceinline__ PairGeo coop_geo(const MixArgs& a, const WarpOwn& ow,
   g.meta = 0;
   g.pad = 0;
   if (WET || coarse < a.coarse_tol) {
-    const float4 lj = ro(a.plo_in + j);
-    g.rj = hj.w + lj.w;
-    const float bx = lo.x - lj.x, by = lo.y - lj.y, bz = lo.z - lj.z;
-    /* d^2 - S^2 from exact pieces */
-    const float px = ax * ax, py = ay * ay, pz = az * az;
-    const float ex = fmaf(ax, ax, -px), ey = fmaf(ay, ay, -py), ez = fmaf(az, az, -pz);
-    float t1, t2, es;
-    const float s1 = two_sum(px, py, t1);
-    const float s2 = two_sum(s1, pz, t2);
-    const float slo = (lo.w + lj.w);
-    const float Sh = two_sum(hi.w, hj.w, es);
-    const float Sl = es + slo;
-    const float qq2 = Sh * Sh, eq = fmaf(Sh, Sh, -qq2);
-    const float s3 = s2 - qq2;
-    const float small = (t1 + t2) + (ex + ey + ez - eq) + 2.0f * (ax * bx + ay * by + az * bz) -
-                        2.0f * Sh * Sl + (bx * bx + by * by + bz * bz) - Sl * Sl;
-    const float D = s3 + small;
-    const float dx = ax + bx, dy = ay + by, dz = az + bz;
-    const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
-    g.gap = __fdividef(D, dist + (Sh + Sl));
-    const float inv = __frcp_rn(dist);
-    g.ux = dx * inv;
-    g.uy = dy * inv;
-    g.uz = dz * inv;
+    float3 u;
+    g.gap = exact_gap(hi, lo, hj, ro(a.plo_in + j), ax, ay, az, u, g.rj);
+    g.ux = u.x;
+    g.uy = u.y;
+    g.uz = u.z;
     if (g.gap < 0.f) g.meta = kGContact;
   }
   if (WET && wet_o) {
@@ -862,18 +860,11 @@ __device__ __forceinline__ PairGeo coop_geo(const MixArgs& a, const WarpOwn& ow,
 /* phase B for one contact: the elasto-plastic law with its history record */
 __device__ __forceinline__ PairOut coop_contact(const MixArgs& a, const WarpOwn& ow, int o, long long s,
                                                 const PairGeo& g) {
-  const float4 vj4 = ro(a.v_in + g.j), wj4 = ro(a.w_in + g.j);
-  MixedRec rc = load_rec(a.rec + s);
   const float4 hi = ow.hi[o], lo = ow.lo[o], vi = ow.v[o], wi = ow.w[o];
-  const float ri = hi.w + lo.w, rj = g.rj;
-  const float3 u = f3(g.ux, g.uy, g.uz);
-  const float3 cpv = (f3(vi.x - vj4.x, vi.y - vj4.y, vi.z - vj4.z)) -
-                     crossf(f3(wi.x, wi.y, wi.z) * ri + f3(wj4.x, wj4.y, wj4.z) * rj, u);
-  const float ijRad = ri * rj / (ri + rj);
   float3 dF, dM;
   float dR;
-  law32(a.pp, ijRad, -g.gap, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
-  store_rec(a.rec + s, rc);
+  pp_contact(a.pp, a.rec + s, hi.w + lo.w, g.rj, f3(vi.x, vi.y, vi.z), f3(wi.x, wi.y, wi.z), ro(a.v_in + g.j),
+             ro(a.w_in + g.j), f3(g.ux, g.uy, g.uz), g.gap, a.rfrc, a.dtf, dF, dM, dR);
   return PairOut{dF.x, dF.y, dF.z, dM.x, dM.y, dM.z, dR, kPContact};
 }
 
