@@ -578,7 +578,14 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
     return fail(DEM_ERR_ARG, "dem_create: level particle counts do not add up to np");
   }
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking);
+  for (cudaEvent_t& ev : c->xev)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   if (e != cudaSuccess) {
+    for (cudaEvent_t ev : c->xev)
+      if (ev) cudaEventDestroy(ev);
+    if (c->xfer) cudaStreamDestroy(c->xfer);
+    if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return cuda_check(e, "cudaStreamCreate");
   }
@@ -696,6 +703,8 @@ extern "C" dem_status dem_destroy(dem_ctx* c) {
   destroy_graph(c);
   if (c->mx) mixed_destroy(c);
   for (void* p : c->allocs) cudaFree(p);
+  for (cudaEvent_t ev : c->xev) cudaEventDestroy(ev);
+  cudaStreamDestroy(c->xfer);
   cudaStreamDestroy(c->stream);
   delete c;
   return DEM_OK;
@@ -718,6 +727,7 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
   if (e == cudaSuccess && vel) e = cudaMemcpyAsync(b.tmp_vel, vel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && angvel)
     e = cudaMemcpyAsync(b.tmp_angv, angvel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->xev[0], c->stream);
   if (e != cudaSuccess) return cuda_check(e, "dem_set_state upload");
   k_import<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_pos, b.tmp_vel, b.tmp_angv, b.pos, b.vel,
                                                          b.angv, vel != nullptr, angvel != nullptr);
@@ -731,7 +741,9 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
     if (st == DEM_OK) st = mixed_shadows(c, c->parity, c->stream);
     if (st != DEM_OK) return st;
   }
-  e = cudaStreamSynchronize(c->stream);
+  /* the caller's arrays are free again once the copies are done; the import
+   * and the shadows run on behind them, ahead of the next step */
+  e = cudaEventSynchronize(c->xev[0]);
   return cuda_check(e, "dem_set_state");
 }
 
@@ -749,22 +761,27 @@ extern "C" dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, doub
     const double3* dev;
   } items[5] = {{pos, b.pos}, {vel, b.vel}, {angvel, b.angv}, {force, b.force}, {mom, b.mom}};
   /* caller order: each array gathered through the inverse of the cell order
-   * into its own staging buffer, then every copy to the host queued behind
-   * the gathers and one wait for all of them */
+   * into its own staging buffer on the compute stream; its copy to the host
+   * starts on the copy stream as soon as that gather is done, while the next
+   * array is gathered; the compute stream then waits for the copies (the
+   * staging buffers are reused by the next import), the host for the last */
   double3* stage[5] = {b.tmp_pos, b.tmp_vel, b.tmp_angv, b.tmp_out, b.tmp_out + N};
   k_inverse<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_id);
   int k = 0;
+  cudaError_t e = cudaSuccess;
   for (auto& it : items) {
-    if (!it.host) continue;
-    k_export_gather<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.tmp_id, it.dev, stage[k++]);
+    if (!it.host || e != cudaSuccess) continue;
+    k_export_gather<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.tmp_id, it.dev, stage[k]);
+    e = cudaEventRecord(c->xev[1 + k], c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->xfer, c->xev[1 + k], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(it.host, stage[k], sizeof(double3) * N, cudaMemcpyDeviceToHost, c->xfer);
+    k++;
   }
-  k = 0;
-  for (auto& it : items) {
-    if (!it.host) continue;
-    cudaError_t e = cudaMemcpyAsync(it.host, stage[k++], sizeof(double3) * N, cudaMemcpyDeviceToHost, c->stream);
-    if (e != cudaSuccess) return cuda_check(e, "dem_get_state");
-  }
-  return cuda_check(cudaStreamSynchronize(c->stream), "dem_get_state");
+  if (e == cudaSuccess) e = cudaEventRecord(c->xev[6], c->xfer);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->xev[6], 0);
+  if (e != cudaSuccess) return cuda_check(e, "dem_get_state");
+  return cuda_check(cudaEventSynchronize(c->xev[6]), "dem_get_state");
 }
 
 extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {

@@ -74,6 +74,11 @@ struct dem_ctx {
   int n;
   long long slots;
   cudaStream_t stream;
+  /* host transfers: the copy stream and its events (xev[0]: the upload's
+   * copies done; xev[1..5]: an export array gathered; xev[6]: the export's
+   * copies done) */
+  cudaStream_t xfer;
+  cudaEvent_t xev[7];
   dem::DevConsts k;
   dem::LevelView lv;
   int lstart[DEM_MAX_LEVELS];

@@ -299,7 +299,9 @@ dem_status dem_create(const dem_setup* s, const double* rad, const int* plevel,
                       const int* nebor_idx, const dem_options* opt, dem_ctx** out);
 dem_status dem_destroy(dem_ctx* c);
 /* Host state in the reference's double3 layout and particle order (reduced
- * units).  vel/angvel may be NULL (zero).  Marks the lists for rebuild. */
+ * units).  vel/angvel may be NULL (zero).  Marks the lists for rebuild.
+ * Returns once the caller's arrays have been read; the device work behind
+ * the copies stays queued on the context's stream. */
 dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel);
 /* As dem_set_state, but with request_rebuild = 0 the current neighbour lists,
  * contact history and path-length accumulators are kept: for callers that
@@ -307,7 +309,8 @@ dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, con
  * valid as long as no particle moved by more than the skin allowance). */
 dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel,
                             int request_rebuild);
-/* Any pointer may be NULL.  force/mom are the last step's totals. */
+/* Any pointer may be NULL.  force/mom are the last step's totals.  Returns
+ * when every requested array is written. */
 dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,
                          double3* mom);
 /* Advance nsteps time steps.  Device-resident; no host synchronisation inside
