@@ -783,6 +783,35 @@ struct LaneAcc {
 };
 static_assert(sizeof(LaneAcc) == 80, "LaneAcc is 80 bytes");
 
+/* a pass's pair geometry and pair results in shared memory, each pair as two
+ * 16-byte halves in two arrays, so that a warp's 32 consecutive pairs are 16
+ * bytes apart: one 128-bit access a quarter-warp per wavefront, no bank
+ * conflicts (a 32-byte record would take two) */
+struct PairBuf {
+  float4* gu; /* ux, uy, uz, gap */
+  int4* gm;   /* j, rj (bits), meta, pad */
+  float4* oa; /* fx, fy, fz, mx */
+  float4* ob; /* my, mz, rr, flags (bits) */
+  __device__ __forceinline__ void put_geo(int k, const PairGeo& g) const {
+    gu[k] = make_float4(g.ux, g.uy, g.uz, g.gap);
+    gm[k] = make_int4(g.j, __float_as_int(g.rj), g.meta, g.pad);
+  }
+  __device__ __forceinline__ PairGeo geo(int k) const {
+    const float4 u = gu[k];
+    const int4 m = gm[k];
+    return PairGeo{u.x, u.y, u.z, u.w, m.x, __int_as_float(m.y), m.z, m.w};
+  }
+  __device__ __forceinline__ int meta(int k) const { return reinterpret_cast<const int*>(gm + k)[2]; }
+  __device__ __forceinline__ void put_out(int k, const PairOut& r) const {
+    oa[k] = make_float4(r.fx, r.fy, r.fz, r.mx);
+    ob[k] = make_float4(r.my, r.mz, r.rr, __int_as_float(r.flags));
+  }
+  __device__ __forceinline__ PairOut out(int k) const {
+    const float4 x = oa[k], y = ob[k];
+    return PairOut{x.x, x.y, x.z, x.w, y.x, y.y, y.z, __float_as_int(y.w)};
+  }
+};
+
 #ifndef DEM_COOP_CHUNK
 #define DEM_COOP_CHUNK 64
 #endif
@@ -795,8 +824,8 @@ struct Coop {
   static constexpr int kChunk = NET ? 64 : DEM_COOP_CHUNK;
   static constexpr size_t kOffAcc = sizeof(WarpOwn);
   static constexpr size_t kOffGeo = kOffAcc + 32 * sizeof(LaneAcc);
-  static constexpr size_t kOffOut = kOffGeo + sizeof(PairGeo) * kChunk;
-  static constexpr size_t kOffQ = kOffOut + sizeof(PairOut) * kChunk;
+  static constexpr size_t kOffOut = kOffGeo + 32 * kChunk; /* PairBuf: two 16-byte halves per pair */
+  static constexpr size_t kOffQ = kOffOut + 32 * kChunk;
   static constexpr size_t kOffList = kOffQ + (NET ? sizeof(CapEntry) * kChunk : 0);
   static constexpr size_t kWarpBytes = kOffList + 2 * kChunk;
   static constexpr size_t smem(int warps) {
@@ -911,14 +940,14 @@ __device__ __forceinline__ void coop_bridge(const MixArgs& a, const WarpOwn& ow,
 
 /* run the pass's bridge queue through the network, then fold each entry into
  * its pair's result: rupture decision, bridge flag, force */
-__device__ __forceinline__ void cap_fold_coop(const CapNetSmem& w, CapEntry* qw, int qn, PairOut* pb,
+__device__ __forceinline__ void cap_fold_coop(const CapNetSmem& w, CapEntry* qw, int qn, const PairBuf& pb,
                                               unsigned char* brg) {
   cap_run_queue(w, qw, qn);
   for (int e = threadIdx.x & 31; e < qn; e += 32) {
     const CapEntry en = qw[e];
     const int b = (en.meta & 1) ? 1 : (en.gap > en.vol ? 0 : 1);
     brg[en.slot] = (unsigned char)b;
-    PairOut& r = pb[en.meta >> 8];
+    PairOut r = pb.out(en.meta >> 8);
     int fl = r.flags | kPMlp;
     if (b) {
       r.fx += en.wx * en.sep;
@@ -927,6 +956,7 @@ __device__ __forceinline__ void cap_fold_coop(const CapNetSmem& w, CapEntry* qw,
       fl |= kPWet | (en.gap >= 0.f ? kPNbr : 0);
     }
     r.flags = fl;
+    pb.put_out(en.meta >> 8, r);
   }
   __syncwarp();
 }
@@ -952,8 +982,8 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
   unsigned char* wsm = dsm + (NET ? ((sizeof(CapNetSmem) + 15) / 16) * 16 : 0) + (threadIdx.x >> 5) * CF::kWarpBytes;
   WarpOwn& ow = *reinterpret_cast<WarpOwn*>(wsm);
   LaneAcc* acc = reinterpret_cast<LaneAcc*>(wsm + CF::kOffAcc);
-  PairGeo* geo = reinterpret_cast<PairGeo*>(wsm + CF::kOffGeo);
-  PairOut* pb = reinterpret_cast<PairOut*>(wsm + CF::kOffOut);
+  const PairBuf pb{reinterpret_cast<float4*>(wsm + CF::kOffGeo), reinterpret_cast<int4*>(wsm + CF::kOffGeo + 16 * CH),
+                   reinterpret_cast<float4*>(wsm + CF::kOffOut), reinterpret_cast<float4*>(wsm + CF::kOffOut + 16 * CH)};
   CapEntry* qw = reinterpret_cast<CapEntry*>(wsm + CF::kOffQ);
   unsigned char* clist = wsm + CF::kOffList;
   unsigned char* blist = clist + CH;
@@ -1048,7 +1078,7 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
         int meta = 0;
         if (act) {
           const PairGeo g = coop_geo<WET>(a, ow, o, (wetm >> o) & 1u, s, j, hj);
-          geo[p - c0] = g;
+          pb.put_geo(p - c0, g);
           meta = g.meta;
           if (meta & kGContact) { /* phase B will need them: start bringing them in */
             prefetch_l2(a.rec + s);
@@ -1077,7 +1107,7 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
       const int p = c0 + pidx;
       const int o = coop_owner(incl, p);
       const int eo = __shfl_sync(FULL, excl, o);
-      if (k < nc) pb[pidx] = coop_contact(a, ow, o, coop_slot(ow, o, p, eo), geo[pidx]);
+      if (k < nc) pb.put_out(pidx, coop_contact(a, ow, o, coop_slot(ow, o, p, eo), pb.geo(pidx)));
     }
     __syncwarp();
     /* ---- C: the bridges over the compacted list ---- */
@@ -1092,12 +1122,12 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
         bool want = false;
         CapEntry ent;
         if (k < nb) {
-          const PairGeo g = geo[pidx];
+          const PairGeo g = pb.geo(pidx);
           PairOut r;
-          if (g.meta & kGContact) r = pb[pidx];
+          if (g.meta & kGContact) r = pb.out(pidx);
           else r = PairOut{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
           coop_bridge<NET>(a, ow, o, coop_slot(ow, o, p, eo), g, r, capw, pidx, want, ent);
-          pb[pidx] = r;
+          pb.put_out(pidx, r);
         }
         if (NET) {
           const unsigned m = __ballot_sync(FULL, want);
@@ -1113,8 +1143,8 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
     if (k0 < k1) {
       LaneAcc A = acc[lane];
       for (int kk = k0; kk < k1; kk++) {
-        if (!(geo[kk - c0].meta & (kGContact | kGBridge))) continue;
-        const PairOut r = pb[kk - c0];
+        if (!(pb.meta(kk - c0) & (kGContact | kGBridge))) continue;
+        const PairOut r = pb.out(kk - c0);
         if (r.flags & (kPContact | kPWet)) A.F.add(f3(r.fx, r.fy, r.fz));
         if (r.flags & kPContact) {
           A.M.add(f3(r.mx, r.my, r.mz));
