@@ -5,7 +5,9 @@ the FP64 reference-formula kernels (build.cu, step64.cu) are compiled with
 -fmad=false so their arithmetic rounds like the CPU oracle's; the mixed
 precision kernel keeps FMA contraction and takes the hardware FP32 square
 root, division and exponentials (-use_fast_math: errors of a few ulp, far
-below its FP32 force tolerance; its FP64 arithmetic is unaffected).  No cmake, no torch extension: the
+below its FP32 force tolerance; its FP64 arithmetic is unaffected).  The
+step-chaining unit launches graphs from the device and is the one unit built
+with relocatable device code (nvcc's link step adds the device link).  No cmake, no torch extension: the
 library exposes a plain C ABI (include/heydem_gb300.h).
 """
 from __future__ import annotations
@@ -38,6 +40,7 @@ UNITS = [
     ("capnet.cu", []),
     ("tune.cu", []),
     ("feed.cu", []),
+    ("chain.cu", ["-rdc=true"]),
 ]
 
 
@@ -84,7 +87,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with cf.ThreadPoolExecutor(max_workers=min(len(units), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda u: _compile(u[0], u[1], verbose), units))
     tmp = OUT.with_suffix(".so.tmp")
-    cmd = [nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudadevrt", "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

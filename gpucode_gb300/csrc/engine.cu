@@ -335,11 +335,15 @@ dem_status enqueue_step(dem_ctx* c, cudaStream_t s, int parity) {
 
 void destroy_graph(dem_ctx* c) {
   for (int p = 0; p < 2; p++) {
-    if (c->graph_exec[p]) cudaGraphExecDestroy(c->graph_exec[p]);
-    if (c->graph_one[p]) cudaGraphExecDestroy(c->graph_one[p]);
-    c->graph_exec[p] = nullptr;
-    c->graph_one[p] = nullptr;
+    cudaGraphExec_t* all[5] = {&c->graph_exec[p], &c->graph_one[p], &c->chain_step[p], &c->chain_single[p],
+                               &c->chain_rebuild[p]};
+    for (cudaGraphExec_t* g : all) {
+      if (*g) cudaGraphExecDestroy(*g);
+      *g = nullptr;
+    }
   }
+  /* rebuilt on the next step against the new configuration */
+  if (c->chain_state > 0) c->chain_state = 0;
 }
 
 /* G steps: [decide -> IF(rebuild) -> step] x G; the mixed path's shadow
@@ -411,6 +415,78 @@ dem_status build_graph(dem_ctx* c, int G, int start_parity, cudaGraphExec_t* out
   }
   cudaGraphDestroy(g);
   cudaStreamDestroy(cs);
+  return st;
+}
+
+/* capture what `enqueue` puts on a stream into a graph instantiated for
+ * device launch and uploaded */
+template <class F>
+dem_status capture_device_graph(dem_ctx* c, F enqueue, cudaGraphExec_t* out) {
+  cudaStream_t cs;
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_check(e, "capture stream");
+  cudaGraph_t g = nullptr;
+  dem_status st = DEM_OK;
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    st = enqueue(cs);
+    const cudaError_t ee = cudaStreamEndCapture(cs, &g);
+    if (st == DEM_OK && ee != cudaSuccess) st = cuda_check(ee, "end capture");
+  } else {
+    st = cuda_check(e, "begin capture");
+  }
+  if (st == DEM_OK) {
+    e = cudaGraphInstantiateWithFlags(out, g, cudaGraphInstantiateFlagDeviceLaunch);
+    if (e == cudaSuccess) e = cudaGraphUpload(*out, c->stream);
+    if (e != cudaSuccess) st = cuda_check(e, "device graph instantiate");
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
+  return st;
+}
+
+/* the chained step graphs of the mixed path: S[p] (countdown), S1[p] (one
+ * step), R[p] (rebuild), and the control block that names them */
+dem_status build_chain(dem_ctx* c) {
+  EngineBufs& b = c->b;
+  dem_status st = DEM_OK;
+  if (!c->chain_ctl) {
+    void* p = nullptr;
+    st = cuda_alloc(&p, sizeof(StepCtl));
+    if (st != DEM_OK) return st;
+    c->allocs.push_back(p);
+    c->chain_ctl = (StepCtl*)p;
+  }
+  for (int p = 0; p < 2 && st == DEM_OK; p++) {
+    st = capture_device_graph(
+        c,
+        [&](cudaStream_t cs) {
+          dem_status r = chain_clear_request(b.flag, b.need, cs);
+          return r == DEM_OK ? enqueue_rebuild(c, cs, p) : r;
+        },
+        &c->chain_rebuild[p]);
+    for (int single = 0; single < 2 && st == DEM_OK; single++) {
+      st = capture_device_graph(
+          c,
+          [&](cudaStream_t cs) {
+            c->step_gate = b.need;
+            dem_status r = enqueue_step(c, cs, p);
+            c->step_gate = nullptr;
+            return r == DEM_OK ? chain_launch_tail(c->chain_ctl, b.flag, b.need, b.err, p, single != 0, cs) : r;
+          },
+          single ? &c->chain_single[p] : &c->chain_step[p]);
+    }
+  }
+  if (st == DEM_OK) {
+    StepCtl h;
+    std::memset(&h, 0, sizeof(h));
+    for (int p = 0; p < 2; p++) {
+      h.step[p] = c->chain_step[p];
+      h.single[p] = c->chain_single[p];
+      h.rebuild[p] = c->chain_rebuild[p];
+    }
+    st = cuda_check(cudaMemcpy(c->chain_ctl, &h, sizeof(h), cudaMemcpyHostToDevice), "step chain control");
+  }
   return st;
 }
 
@@ -712,6 +788,8 @@ extern "C" dem_status dem_destroy(dem_ctx* c) {
 
 extern "C" void* dem_stream(dem_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
+extern "C" int dem_step_chained(dem_ctx* c) { return c && c->chain_state == 1 ? 1 : 0; }
+
 extern "C" dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel) {
   return dem_set_state_ex(c, pos, vel, angvel, 1);
 }
@@ -788,6 +866,37 @@ extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return fail(DEM_ERR_ARG, "dem_step: bad argument");
   dem_status st = DEM_OK;
   int left = nsteps;
+  if (c->opt.use_graph && c->opt.precision == DEM_PREC_MIXED && c->n > 0 && c->chain_state >= 0 && nsteps > 0) {
+    /* steps chained on the device: one host launch for the whole call */
+    if (c->chain_state == 0) {
+      st = build_chain(c);
+      if (st == DEM_OK) {
+        c->chain_state = 1;
+      } else {
+        /* this device or driver cannot launch these graphs from the device:
+         * keep the conditional-node graphs */
+        destroy_graph(c);
+        c->chain_state = -1;
+        cudaGetLastError();
+      }
+    }
+    if (c->chain_state == 1) {
+      const int p = c->parity;
+      cudaError_t e;
+      if (nsteps == 1) {
+        e = cudaGraphLaunch(c->chain_single[p], c->stream);
+      } else {
+        st = chain_set_left(c->chain_ctl, nsteps, c->stream);
+        if (st != DEM_OK) return st;
+        e = cudaGraphLaunch(c->chain_step[p], c->stream);
+      }
+      if (e != cudaSuccess) return cuda_check(e, "cudaGraphLaunch");
+      c->iter += nsteps;
+      c->ctime += nsteps * c->s.sim.dt;
+      c->parity ^= (nsteps & 1);
+      return DEM_OK;
+    }
+  }
   if (c->opt.use_graph) {
     const int G = graph_len(c);
     const bool mixed = c->opt.precision == DEM_PREC_MIXED;
@@ -941,6 +1050,7 @@ extern "C" dem_status dem_sync(dem_ctx* c) {
   if (err & 1) return fail(DEM_ERR_OVERFLOW, "a neighbour list ran past its level's slot capacity");
   if (err & 2) return fail(DEM_ERR_NONFINITE, "non-finite particle state");
   if (err & 4) return fail(DEM_ERR_CELL, "a particle left the cell grid");
+  if (err & 8) return fail(DEM_ERR_CUDA, "a step chained on the device could not launch the next graph");
   return DEM_OK;
 }
 
@@ -1060,8 +1170,13 @@ extern "C" dem_status dem_get_aux(dem_ctx* c, double* pmove, int* lqd, int* nwal
   if (e == cudaSuccess) e = cudaMemcpy(wl.data(), c->b.wlist, sizeof(int) * 3 * N, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(wr.data(), c->b.wrec, sizeof(ContactRec) * 3 * N, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(id.data(), c->b.id, sizeof(int) * N, cudaMemcpyDeviceToHost);
+  int nd = 0;
   if (e == cudaSuccess) e = cudaMemcpy(&fl, c->b.flag, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&nd, c->b.need, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_check(e, "dem_get_aux");
+  /* a step chained on the device hands its move flag on as the rebuild
+   * request: either one means the next step rebuilds first */
+  if (fl <= 0 && nd != 0) fl = 1;
   for (size_t q = 0; q < N; q++) {
     const int i = id[q];
     if (pmove) pmove[i] = pm[q];

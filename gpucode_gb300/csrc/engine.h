@@ -30,6 +30,15 @@ namespace dem {
 
 struct MixedState; /* mixed.cu */
 
+/* device-side step chaining (chain.cu): the device-launchable graphs of one
+ * step (with and without the countdown) and of a rebuild, per shadow parity,
+ * and the countdown of the running chain */
+struct StepCtl {
+  int left;
+  int pad;
+  cudaGraphExec_t step[2], single[2], rebuild[2];
+};
+
 struct EngineBufs {
   /* particle state */
   double3 *pos, *vel, *angv;
@@ -94,6 +103,14 @@ struct dem_ctx {
   cudaGraphExec_t graph_one[2];
   int parity; /* mixed: which shadow buffer the next step reads */
   int moving_walls; /* a cylinder's top wall moves (topv != 0): moved before every step's wall contacts */
+  /* device-side step chaining (mixed precision): 0 not built yet, 1 built,
+   * -1 unavailable (the conditional-node graphs run instead); the graphs; the
+   * control block on the device; and, while a chained step is captured, the
+   * rebuild request word that gates its kernels (NULL otherwise) */
+  int chain_state;
+  cudaGraphExec_t chain_step[2], chain_single[2], chain_rebuild[2];
+  dem::StepCtl* chain_ctl;
+  const int* step_gate;
   /* dem_profile_kernels: when set, the rebuild and the step record an event
    * after each of their kernels (NULL otherwise, and always during capture) */
   std::vector<std::pair<const char*, cudaEvent_t>>* marks;
@@ -119,5 +136,11 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s);
 dem_status mixed_pre_rebuild(dem_ctx* c, int which, cudaStream_t s);
 /* download the last step's force totals into the FP64 force array */
 dem_status mixed_force_to_master(dem_ctx* c, cudaStream_t s);
+
+/* chain.cu: the chaining kernel after a step (tail-launches the rebuild and
+ * the next step), the countdown, and the reset of the rebuild request */
+dem_status chain_launch_tail(StepCtl* ctl, int* flag, int* need, int* err, int parity, bool single, cudaStream_t s);
+dem_status chain_set_left(StepCtl* ctl, int nsteps, cudaStream_t s);
+dem_status chain_clear_request(int* flag, int* need, cudaStream_t s);
 
 }  // namespace dem

@@ -99,6 +99,9 @@ struct MixArgs {
   const CapNetSmem* capw;
   unsigned long long theta_seed;
   float theta_max;
+  /* a step chained on the device: the rebuild request word; when it is set
+   * the step does nothing (it runs again after the rebuild).  NULL otherwise */
+  const int* gate;
 };
 
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
@@ -572,7 +575,7 @@ __device__ __forceinline__ void finish_particle(const MixArgs& a, int q, int qq,
 
 template <bool WET, bool NET>
 __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArgs a) {
-  if (a.n <= 0) return;
+  if (a.n <= 0 || (a.gate && *a.gate)) return;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = q < a.n;
   const int qq = live ? q : a.n - 1;
@@ -968,7 +971,7 @@ __device__ __forceinline__ long long coop_slot(const WarpOwn& ow, int o, int p, 
 
 template <bool WET, bool NET>
 __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_step_coop(MixArgs a) {
-  if (a.n <= 0) return;
+  if (a.n <= 0 || (a.gate && *a.gate)) return;
   using CF = Coop<NET>;
   constexpr int CH = CF::kChunk;
   const unsigned FULL = 0xffffffffu;
@@ -1171,8 +1174,10 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
 }
 
 /* CirPWInterG's wall motion (kernel.cu:966-969): every cylinder's top wall
- * moves by topv dt before any particle meets it this step */
-__global__ void k_move_walls(CylinderBC* cyl, int n_cyl, double dt) {
+ * moves by topv dt before any particle meets it this step (not in a chained
+ * step that waits for a rebuild: it moves them when it runs again) */
+__global__ void k_move_walls(CylinderBC* cyl, int n_cyl, double dt, const int* gate) {
+  if (gate && *gate) return;
   for (int k = threadIdx.x; k < n_cyl; k += blockDim.x) cyl[k].Tw = cyl[k].Tw + cyl[k].topv * dt;
 }
 
@@ -1336,6 +1341,7 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   a.capw = reinterpret_cast<const CapNetSmem*>(c->cap_w);
   a.theta_seed = c->theta_seed;
   a.theta_max = c->theta_max;
+  a.gate = c->step_gate;
   /* threads per block: the option (a multiple of 32 up to 128), else 128 */
   const int ob = c->opt.block_size;
   const int bs = (ob >= 32 && ob <= 32 * kWarps && ob % 32 == 0) ? ob : 32 * kWarps;
@@ -1343,7 +1349,7 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   if (net && !c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
   const int g = grid_for(c->n, bs);
   if (c->moving_walls) {
-    k_move_walls<<<1, 32, 0, s>>>(b.cyl, b.n_sys > 0 ? b.n_sys : 1, c->s.prm.dt);
+    k_move_walls<<<1, 32, 0, s>>>(b.cyl, b.n_sys > 0 ? b.n_sys : 1, c->s.prm.dt, c->step_gate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_check(e, "mixed_step wall motion");
   }

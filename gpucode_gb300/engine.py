@@ -150,6 +150,10 @@ class Engine:
     def stream(self) -> int:
         return int(self.lib.dem_stream(self.h) or 0)
 
+    def step_chained(self) -> bool:
+        """whether the steps launch one another on the device (after the first step)"""
+        return bool(self.lib.dem_step_chained(self.h))
+
     def neighbors(self, max_per: int = 256) -> tuple[np.ndarray, np.ndarray]:
         counts = np.zeros(self.n, np.int32)
         partners = np.full((self.n, max_per), -1, np.int32)

@@ -332,6 +332,10 @@ dem_status dem_sync(dem_ctx* c);
 dem_status dem_get_stats(dem_ctx* c, dem_stats* st);
 /* The context's CUDA stream (cudaStream_t) for callers that time or order work. */
 void* dem_stream(dem_ctx* c);
+/* 1 when the context's steps launch one another on the device (mixed
+ * precision with graphs, after the first dem_step), 0 when they run as
+ * host-launched graphs with a conditional rebuild node or host-driven. */
+int dem_step_chained(dem_ctx* c);
 /* Current neighbour lists in the reference's terms: for every particle i (in
  * the caller's order) its partners (caller's ids) in the reference's list order.
  * counts[np]; partners[np*max_per] (row i = partners of i).  Returns
@@ -344,8 +348,9 @@ dem_status dem_get_history(dem_ctx* c, double* rec, int* brg, int max_per);
 /* The rest of the per-particle state, in the caller's order: path length since
  * the last rebuild pmove[np], last step's bridge count lqd[np], wall list
  * nwall[np] / wlist[np][3] (0 top, 1 bottom, 2 lateral) with its records
- * wrec[np][3][8] (as dem_get_history), and the pending rebuild flag.  Any
- * pointer may be NULL. */
+ * wrec[np][3][8] (as dem_get_history), and the pending rebuild flag (the
+ * count of particles past the move limit, or 1 for a rebuild requested
+ * otherwise; 0: the next step keeps the lists).  Any pointer may be NULL. */
 dem_status dem_get_aux(dem_ctx* c, double* pmove, int* lqd, int* nwall, int* wlist, double* wrec, int* flag);
 /* Batched systems (no counterpart in the reference): the context's particles
  * belong to n_sys independent packings laid out side by side in its domain

@@ -131,6 +131,34 @@ def test_graph_replay_equals_host_stepping(cuda, precision):
     assert np.array_equal(ha[0], hb[0]) and np.array_equal(ha[1], hb[1])
 
 
+def test_device_chained_steps_equal_single_and_host_steps(cuda):
+    """mixed precision with graphs chains its steps on the device (the step
+    graph tail-launches the rebuild and the next step): one 240-step call,
+    240 one-step calls, calls of uneven lengths and host-driven stepping give
+    the same bits, with the rebuilds at the same steps"""
+    w = _workloads.small_wet()
+    pos, vel, ang = _workloads.stirred(w)
+    runs = {"chain": [240], "single": [1] * 240, "uneven": [100, 1, 37, 1, 101], "host": [240]}
+    out = {}
+    for name, calls in runs.items():
+        e = Engine(w.setup, precision="mixed", use_graph=name != "host")
+        e.set_state(pos, vel, ang)
+        for k in calls:
+            e.step(k)
+        e.sync()
+        assert e.step_chained() == (name != "host")
+        out[name] = (e.get_state(), e.stats()["rebuilds"], e.history(_lockstep.max_per(w)))
+        e.close()
+    s0, r0, h0 = out["host"]
+    assert r0 >= 2
+    for name in ("chain", "single", "uneven"):
+        s, r, h = out[name]
+        assert r == r0, name
+        for k in ("pos", "vel", "angvel", "force"):
+            assert np.array_equal(s[k], s0[k]), (name, k)
+        assert np.array_equal(h[0], h0[0]) and np.array_equal(h[1], h0[1]), name
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_checkpoint_resume_is_bit_exact(cuda, tmp_path, precision):
     w = _workloads.small_wet()
