@@ -593,6 +593,10 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
   prefetch_l2(a.vel + qq);
   prefetch_l2(a.angv + qq);
   prefetch_l2(a.pmove + qq);
+  /* so are the wall count and list, which would otherwise be two dependent
+   * DRAM misses at the end of the warp's work */
+  prefetch_l2(a.nwall + qq);
+  prefetch_l2(a.wlist + 3 * qq);
 
   const float4 hi = ro(a.phi_in + qq), lo = ro(a.plo_in + qq), vi4 = ro(a.v_in + qq), wi4 = ro(a.w_in + qq);
   const float ri = hi.w + lo.w;
@@ -638,6 +642,13 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
     if (k + 1 < nn) {
       j_next = ro(a.nebor + s + stride);
       hj_next = ro(a.phi_in + j_next);
+      /* the next pair's lo parts (and, wet, its velocity record and bridge
+       * flag) are read by every candidate: into L2 while this pair runs */
+      prefetch_l2(a.plo_in + j_next);
+      if (WET) {
+        prefetch_l2(a.v_in + j_next);
+        prefetch_l2(a.brg + s + stride);
+      }
     }
     const float ax = hi.x - hj.x, ay = hi.y - hj.y, az = hi.z - hj.z; /* exact */
     const float shi = hi.w + hj.w;
@@ -999,6 +1010,10 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
   prefetch_l2(a.vel + qq);
   prefetch_l2(a.angv + qq);
   prefetch_l2(a.pmove + qq);
+  /* so are the wall count and list, which would otherwise be two dependent
+   * DRAM misses at the end of the warp's work */
+  prefetch_l2(a.nwall + qq);
+  prefetch_l2(a.wlist + 3 * qq);
 
   const int sys = a.sys_of_id ? a.sys_of_id[ro(a.id + qq)] : 0;
   const int nn = live ? ro(a.num_nebor + qq) : 0;
@@ -1077,6 +1092,9 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
           sn = coop_slot(ow, on, pn, eon);
           jn = ro(a.nebor + sn);
           hjn = ro(a.phi_in + jn);
+          /* its lo parts (read for every candidate) and bridge flag: into L2 now */
+          prefetch_l2(a.plo_in + jn);
+          if (WET) prefetch_l2(a.brg + sn);
         }
         int meta = 0;
         if (act) {
