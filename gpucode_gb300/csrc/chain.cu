@@ -18,7 +18,12 @@
  * and, while steps are left, tail-launches S[1-p].  A tail launch starts when
  * the launching graph has completed, and work queued on the stream after the
  * host's launch waits for the whole chain.  The single-step graphs (one
- * host launch per step) are the same without the countdown.
+ * host launch per step) are the same without the countdown.  For a
+ * one-step call the host launches a second, host-instantiated copy of S1[p]:
+ * launched from the host, a graph instantiated for device launch starts ~5 us
+ * later, and a kernel of the host copy tail-launches the device graphs all the
+ * same (a chain of many steps started from that copy measured ~1.5 us per
+ * step slower, so longer calls launch S[p] itself).
  *
  * need is written only by k_chain and k_clear_request (and by the host
  * between launches), never while a step kernel runs, so every block of a

@@ -335,8 +335,8 @@ dem_status enqueue_step(dem_ctx* c, cudaStream_t s, int parity) {
 
 void destroy_graph(dem_ctx* c) {
   for (int p = 0; p < 2; p++) {
-    cudaGraphExec_t* all[5] = {&c->graph_exec[p], &c->graph_one[p], &c->chain_step[p], &c->chain_single[p],
-                               &c->chain_rebuild[p]};
+    cudaGraphExec_t* all[6] = {&c->graph_exec[p],   &c->graph_one[p],     &c->chain_step[p],
+                               &c->chain_single[p], &c->chain_rebuild[p], &c->chain_single_host[p]};
     for (cudaGraphExec_t* g : all) {
       if (*g) cudaGraphExecDestroy(*g);
       *g = nullptr;
@@ -419,9 +419,10 @@ dem_status build_graph(dem_ctx* c, int G, int start_parity, cudaGraphExec_t* out
 }
 
 /* capture what `enqueue` puts on a stream into a graph instantiated for
- * device launch and uploaded */
+ * device launch and uploaded, and (host_out) into a second instantiation for
+ * launch from the host */
 template <class F>
-dem_status capture_device_graph(dem_ctx* c, F enqueue, cudaGraphExec_t* out) {
+dem_status capture_device_graph(dem_ctx* c, F enqueue, cudaGraphExec_t* out, cudaGraphExec_t* host_out = nullptr) {
   cudaStream_t cs;
   cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_check(e, "capture stream");
@@ -439,6 +440,11 @@ dem_status capture_device_graph(dem_ctx* c, F enqueue, cudaGraphExec_t* out) {
     e = cudaGraphInstantiateWithFlags(out, g, cudaGraphInstantiateFlagDeviceLaunch);
     if (e == cudaSuccess) e = cudaGraphUpload(*out, c->stream);
     if (e != cudaSuccess) st = cuda_check(e, "device graph instantiate");
+  }
+  if (st == DEM_OK && host_out) {
+    e = cudaGraphInstantiate(host_out, g, 0);
+    if (e == cudaSuccess) e = cudaGraphUpload(*host_out, c->stream);
+    if (e != cudaSuccess) st = cuda_check(e, "graph instantiate");
   }
   if (g) cudaGraphDestroy(g);
   cudaStreamDestroy(cs);
@@ -474,7 +480,7 @@ dem_status build_chain(dem_ctx* c) {
             c->step_gate = nullptr;
             return r == DEM_OK ? chain_launch_tail(c->chain_ctl, b.flag, b.need, b.err, p, single != 0, cs) : r;
           },
-          single ? &c->chain_single[p] : &c->chain_step[p]);
+          single ? &c->chain_single[p] : &c->chain_step[p], single ? &c->chain_single_host[p] : nullptr);
     }
   }
   if (st == DEM_OK) {
@@ -884,8 +890,13 @@ extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
       const int p = c->parity;
       cudaError_t e;
       if (nsteps == 1) {
-        e = cudaGraphLaunch(c->chain_single[p], c->stream);
+        /* the host-instantiated copy: it starts sooner, its k_chain
+         * tail-launches the device graphs (rebuild, the step again) all the
+         * same, and work queued after it waits for them */
+        e = cudaGraphLaunch(c->chain_single_host[p], c->stream);
       } else {
+        /* a long chain runs ~1.5 us per step faster started from the
+         * device-launch copy, which outweighs that copy's later start */
         st = chain_set_left(c->chain_ctl, nsteps, c->stream);
         if (st != DEM_OK) return st;
         e = cudaGraphLaunch(c->chain_step[p], c->stream);

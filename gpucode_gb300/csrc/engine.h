@@ -104,11 +104,15 @@ struct dem_ctx {
   int parity; /* mixed: which shadow buffer the next step reads */
   int moving_walls; /* a cylinder's top wall moves (topv != 0): moved before every step's wall contacts */
   /* device-side step chaining (mixed precision): 0 not built yet, 1 built,
-   * -1 unavailable (the conditional-node graphs run instead); the graphs; the
-   * control block on the device; and, while a chained step is captured, the
-   * rebuild request word that gates its kernels (NULL otherwise) */
+   * -1 unavailable (the conditional-node graphs run instead); the graphs
+   * (instantiated for device launch) and a host-instantiated copy of the
+   * one-step graph for dem_step(1) (launched from the host, a device-launch
+   * graph starts ~5 us later); the control block on the device; and, while a
+   * chained step is captured, the rebuild request word that gates its
+   * kernels (NULL otherwise) */
   int chain_state;
   cudaGraphExec_t chain_step[2], chain_single[2], chain_rebuild[2];
+  cudaGraphExec_t chain_single_host[2];
   dem::StepCtl* chain_ctl;
   const int* step_gate;
   /* dem_profile_kernels: when set, the rebuild and the step record an event
