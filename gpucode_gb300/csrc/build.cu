@@ -29,6 +29,7 @@ namespace dem {
 
 namespace {
 
+constexpr int kRowBatch = 8; /* cell rows whose ranges the neighbour search reads at once */
 constexpr int kScanThreads = 256;
 constexpr int kScanPerThread = 8;
 constexpr int kScanTile = kScanThreads * kScanPerThread; /* cells per scan tile */
@@ -112,9 +113,10 @@ __global__ void k_scan_tiles(int* __restrict__ tile_sum, int ntiles) {
 }
 
 /* (2c) cell offsets -> CellStart / CellEnd (-1 for empty cells); count[] is
- * read from cell_end[] and overwritten in place */
+ * read from cell_end[] and overwritten in place.  cell_off (optional, ncells
+ * + 1 entries) receives every cell's offset, empty or not, and the total */
 __global__ void k_cell_ranges(int* __restrict__ cell_start, int* __restrict__ cell_end, int ncells,
-                              const int* __restrict__ tile_off) {
+                              const int* __restrict__ tile_off, int* __restrict__ cell_off) {
   const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanPerThread;
   int c[kScanPerThread];
   int s = 0;
@@ -132,6 +134,10 @@ __global__ void k_cell_ranges(int* __restrict__ cell_start, int* __restrict__ ce
     if (q < ncells) {
       cell_start[q] = c[e] ? off : -1;
       cell_end[q] = c[e] ? off + c[e] : -1;
+      if (cell_off) {
+        cell_off[q] = off;
+        if (q == ncells - 1) cell_off[ncells] = off + c[e];
+      }
     }
     off += c[e];
   }
@@ -183,10 +189,17 @@ __global__ void k_cell_order(const int* __restrict__ sorted_hash, int* __restric
  * from those differences is within pre.tol of the exact one.  A candidate
  * farther than pre.tol from the cut-off is decided in FP32; only the band
  * around it takes the reference's FP64 test, so the list is bit-identical to
- * the all-FP64 build while almost no FP64 square roots are taken. */
+ * the all-FP64 build while almost no FP64 square roots are taken.
+ *
+ * Optional cell_off (every cell's offset in sorted order, empty cells
+ * included, and the total after the last): a row's particles are then
+ * [cell_off[first cell], cell_off[last cell + 1]) -- the same range, in the
+ * same order, from two loads instead of two per cell of the row.  The search
+ * is bound by these scattered loads, not by its arithmetic. */
 __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* __restrict__ rad,
                                 const int* __restrict__ sorted_src, const int* __restrict__ cell_start,
-                                const int* __restrict__ cell_end, const int* __restrict__ plevel,
+                                const int* __restrict__ cell_end, const int* __restrict__ cell_off,
+                                const int* __restrict__ plevel,
                                 const int* __restrict__ nebor_idx, LevelView lv, double3 origin,
                                 double search_gap, int* __restrict__ nebor,
                                 int* __restrict__ num_nebor, int n, int* __restrict__ err, Prefilter pre) {
@@ -202,11 +215,64 @@ __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* _
   const int cap = lv.level_nnebors[L];
   int count = 0;
   bool over = false;
+  /* candidate q (sorted position): the distance test, then the append */
+  auto visit = [&](int q) {
+    const int j = sorted_src ? sorted_src[q] : q;
+    if (j == i) return;
+    bool in = false, decided = false;
+    if (pre.hi) {
+      const float4 hj = pre.hi[j];
+      const float dx = hi_i.x - hj.x, dy = hi_i.y - hj.y, dz = hi_i.z - hj.z;
+      const float dc = sqrtf(dx * dx + dy * dy + dz * dz);
+      const float cut = (hj.w + hi_i.w) + sg;
+      if (dc > cut + pre.tol) decided = true; /* certainly outside */
+      else if (dc < cut - pre.tol) {          /* certainly inside */
+        decided = true;
+        in = true;
+      }
+    }
+    if (!decided) in = len3(sub3(o, pos[j])) < rad[j] + ri + search_gap;
+    if (!in) return;
+    if (count >= cap) {
+      over = true;
+      return;
+    }
+    nebor[base + (long long)count * stride] = j;
+    count++;
+  };
   for (int iL = 0; iL < lv.n_levels; iL++) {
     const int3 g = grid_pos(o, iL, lv, origin);
     const int off = (int)ceil(lv.level_size[L] / lv.level_size[iL]);
     const int cell_sum = iL != 0 ? lv.ncell_idx[iL - 1] : 0;
     const int3 gs = lv.grid_size[iL];
+    if (cell_off) {
+      /* rows r = (z + off) W + (y + off), in the reference's (z, y) order;
+       * the ranges of kRowBatch rows are read with independent loads before
+       * their particles are visited in order */
+      const int W = 2 * off + 1, R = W * W;
+      for (int r0 = 0; r0 < R; r0 += kRowBatch) {
+        int rf[kRowBatch], rl[kRowBatch];
+#pragma unroll
+        for (int b = 0; b < kRowBatch; b++) {
+          rf[b] = rl[b] = 0;
+          const int r = r0 + b;
+          const int z = r / W - off, y = r % W - off;
+          int3 s = make_int3(g.x - off, g.y + y, g.z + z);
+          int3 e = make_int3(g.x + off, g.y + y, g.z + z);
+          if (s.x < 0) s.x = 0;
+          if (e.x > gs.x - 1) e.x = gs.x - 1;
+          if (r < R && !(s.y < 0 || s.z < 0 || s.y > gs.y - 1 || s.z > gs.z - 1) && e.x >= s.x) {
+            const int row = grid_hash(s, iL, lv) + cell_sum;
+            rf[b] = __ldg(cell_off + row);
+            rl[b] = __ldg(cell_off + row + (e.x - s.x) + 1);
+          }
+        }
+#pragma unroll
+        for (int b = 0; b < kRowBatch; b++)
+          for (int q = rf[b]; q < rl[b]; q++) visit(q);
+      }
+      continue;
+    }
     for (int z = -off; z <= off; z++) {
       for (int y = -off; y <= off; y++) {
         int3 s = make_int3(g.x - off, g.y + y, g.z + z);
@@ -227,35 +293,7 @@ __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* _
           if (ce != -1) last = ce;
         }
         if (first == -1 || last == -1) continue;
-        for (int q = first; q < last; q++) {
-          const int j = sorted_src ? sorted_src[q] : q;
-          if (j == i) continue;
-          if (pre.hi) {
-            const float4 hj = pre.hi[j];
-            const float dx = hi_i.x - hj.x, dy = hi_i.y - hj.y, dz = hi_i.z - hj.z;
-            const float dc = sqrtf(dx * dx + dy * dy + dz * dz);
-            const float cut = (hj.w + hi_i.w) + sg;
-            if (dc > cut + pre.tol) continue; /* certainly outside */
-            if (dc < cut - pre.tol) {         /* certainly inside */
-              if (count >= cap) {
-                over = true;
-                continue;
-              }
-              nebor[base + (long long)count * stride] = j;
-              count++;
-              continue;
-            }
-          }
-          const double3 d = sub3(o, pos[j]);
-          if (len3(d) < rad[j] + ri + search_gap) {
-            if (count >= cap) {
-              over = true;
-              continue;
-            }
-            nebor[base + (long long)count * stride] = j;
-            count++;
-          }
-        }
+        for (int q = first; q < last; q++) visit(q);
       }
     }
   }
@@ -385,7 +423,7 @@ size_t sort_scratch_bytes(int np, int ncells) {
 
 dem_status cell_sort(const double3* pos, const int* plevel, const int* order_key, int n, LevelView lv,
                      const DevConsts& k, int ncells, int* sorted_hash, int* sorted_src, int* cell_start,
-                     int* cell_end, void* scratch, int* err, cudaStream_t stream) {
+                     int* cell_end, void* scratch, int* err, cudaStream_t stream, int* cell_off) {
   if (n < 0 || ncells <= 0) return fail(DEM_ERR_ARG, "cell_sort: bad sizes");
   int* key = (int*)scratch;
   int* rank = key + n;
@@ -398,7 +436,7 @@ dem_status cell_sort(const double3* pos, const int* plevel, const int* order_key
                                                       cell_end, err);
   k_tile_sums<<<ntiles, kScanThreads, 0, stream>>>(cell_end, ncells, tile);
   k_scan_tiles<<<1, kScanThreads, 0, stream>>>(tile, ntiles);
-  k_cell_ranges<<<ntiles, kScanThreads, 0, stream>>>(cell_start, cell_end, ncells, tile);
+  k_cell_ranges<<<ntiles, kScanThreads, 0, stream>>>(cell_start, cell_end, ncells, tile, cell_off);
   if (n > 0) {
     k_scatter<<<grid_for(n, 256), 256, 0, stream>>>(key, rank, n, cell_start, sorted_hash, sorted_src);
     k_cell_order<<<grid_for(n, 256), 256, 0, stream>>>(sorted_hash, sorted_src, cell_start, cell_end,
@@ -410,9 +448,9 @@ dem_status cell_sort(const double3* pos, const int* plevel, const int* order_key
 dem_status neighbor_find(const double3* pos, const double* rad, const int* sorted_src,
                          const int* cell_start, const int* cell_end, const int* plevel, const int* nebor_idx,
                          LevelView lv, const DevConsts& k, int* nebor, int* num_nebor, int n, int* err,
-                         cudaStream_t stream, Prefilter pre) {
+                         cudaStream_t stream, Prefilter pre, const int* cell_off) {
   if (n <= 0) return DEM_OK;
-  k_neighbor_find<<<grid_for(n, 128), 128, 0, stream>>>(pos, rad, sorted_src, cell_start, cell_end, plevel,
+  k_neighbor_find<<<grid_for(n, 128), 128, 0, stream>>>(pos, rad, sorted_src, cell_start, cell_end, cell_off, plevel,
                                                        nebor_idx, lv, k.prm.Origin, k.prm.SearchGap, nebor,
                                                        num_nebor, n, err, pre);
   return cuda_check(cudaGetLastError(), "neighbor_find launch");

@@ -102,13 +102,15 @@ size_t sort_scratch_bytes(int np, int ncells);
  *   pos (AoS double3, n particles), plevel, order_key: the particle id the
  *   stable order uses for ties (NULL: the index itself).
  * Outputs sorted hash / sorted source index (position in the input arrays),
- * cell_start/cell_end (-1 for empty cells).  scratch must hold
- * sort_scratch_bytes(n, ncells).  A hash outside [0, ncells) sets bit 4 of
- * *err (may be NULL).  Every launch goes to `stream`. */
+ * cell_start/cell_end (-1 for empty cells) and, if cell_off is not NULL,
+ * every cell's offset in sorted order (ncells + 1 ints, the total last).
+ * scratch must hold sort_scratch_bytes(n, ncells).  A hash outside
+ * [0, ncells) sets bit 4 of *err (may be NULL).  Every launch goes to
+ * `stream`. */
 dem_status cell_sort(const double3* pos, const int* plevel, const int* order_key, int n,
                      LevelView lv, const DevConsts& k, int ncells, int* sorted_hash,
                      int* sorted_src, int* cell_start, int* cell_end, void* scratch, int* err,
-                     cudaStream_t stream);
+                     cudaStream_t stream, int* cell_off = nullptr);
 
 /* FP32 prefilter of the neighbour test (see build.cu): the high floats of
  * (position + offset, radius) and the bound of their distance error */
@@ -119,12 +121,13 @@ struct Prefilter {
 
 /* NeighborFindG semantics (kernel.cu:729-855) on AoS positions; sorted_src
  * maps sorted position -> particle index; writes the level/slot-major list.
- * Slot overflow sets bit 1 of *err and stops appending. */
+ * Slot overflow sets bit 1 of *err and stops appending.  cell_off (from
+ * cell_sort, may be NULL) lets a cell row's range be read with two loads. */
 dem_status neighbor_find(const double3* pos, const double* rad, const int* sorted_src,
                          const int* cell_start, const int* cell_end, const int* plevel,
                          const int* nebor_idx, LevelView lv, const DevConsts& k, int* nebor,
                          int* num_nebor, int n, int* err, cudaStream_t stream,
-                         Prefilter pre = Prefilter{nullptr, 0.f});
+                         Prefilter pre = Prefilter{nullptr, 0.f}, const int* cell_off = nullptr);
 
 /* CirWallListG (kernel.cu:1034-1073); wall list pitched rows.  Batched
  * systems: sys_of_id[id[i]] selects particle i's cylinder in cyl[] (NULL: cyl[0]). */

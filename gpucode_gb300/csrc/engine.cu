@@ -271,7 +271,7 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
                                                b.counters);
   mark(c, s, "k_copy_old");
   st = cell_sort(b.pos, b.plevel, reorder ? b.id : nullptr, n, c->lv, c->k, c->s.sys_ncells, b.sorted_hash,
-                 b.sorted_src, b.cell_start, b.cell_end, b.scratch, b.err, s);
+                 b.sorted_src, b.cell_start, b.cell_end, b.scratch, b.err, s, b.cell_off);
   if (st != DEM_OK) return st;
   mark(c, s, "cell sort (k_hash_count .. k_cell_order)");
   if (reorder) {
@@ -301,7 +301,7 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
     mark(c, s, "k_shadows");
   }
   st = neighbor_find(b.pos, b.rad, reorder ? nullptr : b.sorted_src, b.cell_start, b.cell_end, b.plevel, b.nidx,
-                     c->lv, c->k, b.nebor, b.num_nebor, n, b.err, s, pre);
+                     c->lv, c->k, b.nebor, b.num_nebor, n, b.err, s, pre, b.cell_off);
   if (st != DEM_OK) return st;
   mark(c, s, "k_neighbor_find");
   st = wall_list(b.pos, b.rad, b.cyl, b.wlist, 3 * sizeof(int), b.nwall, n, c->k, s, b.id, b.sys_of_id);
@@ -541,7 +541,7 @@ dem_memory memory_of(long long N, long long S, long long C, const dem_options* o
                    + 3 * 4 + 2 * 4;            /* sorted hash / source, old_to_new, sort scratch */
   if (o && o->precision == DEM_PREC_MIXED) m.per_particle += 9 * 16; /* FP32 shadows */
   m.per_slot = 2 * (4 + 64 + 1);               /* list entry, record, bridge flag, and their copies */
-  m.per_cell = 2 * 4;
+  m.per_cell = 3 * 4;                         /* cell start, end, offset */
   m.slots = S;
   const long long allocations = 64;
   m.total = N * m.per_particle + S * m.per_slot + C * m.per_cell + ((C + 2047) / 2048 + 64) * 4 +
@@ -687,6 +687,7 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   A(b.nebor_old, S); A(b.num_nebor_old, N); A(b.wlist_old, 3 * N); A(b.nwall_old, N); A(b.nidx_old, N);
   A(b.rec, S); A(b.rec_old, S); A(b.brg, S); A(b.brg_old, S); A(b.wrec, 3 * N); A(b.wrec_old, 3 * N);
   A(b.sorted_hash, N); A(b.sorted_src, N); A(b.old_to_new, N); A(b.cell_start, C); A(b.cell_end, C);
+  A(b.cell_off, C + 1);
   A(b.cell_size, L); A(b.grid_size, L); A(b.ncell_idx, L); A(b.npars, L); A(b.nneb, L); A(b.level_size, L);
   A(b.cyl, 1); A(b.flag, 1); A(b.need, 1); A(b.err, 1); A(b.counters, 8);
 #undef A

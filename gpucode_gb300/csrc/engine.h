@@ -58,6 +58,7 @@ struct EngineBufs {
   unsigned char *brg, *brg_old;
   /* sort */
   int *sorted_hash, *sorted_src, *old_to_new, *cell_start, *cell_end;
+  int* cell_off; /* every cell's offset in sorted order, and the total (C + 1) */
   void* scratch;
   /* level tables */
   double* cell_size;
