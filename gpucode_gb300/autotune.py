@@ -14,7 +14,7 @@ from .engine import Setup, _options
 
 
 def autotune(inp, dia, pos_reduced, vel_reduced=None, precision: str = "mixed", capillary: str = "formula",
-             skins=(0.5, 1.0, 2.0), cells=(1.0, 1.3), blocks=(64, 128), warmup: int = 20, trial: int = 200,
+             skins=(0.5, 1.0, 2.0), cells=(1.0, 1.3), blocks=(32, 64, 128), warmup: int = 20, trial: int = 200,
              systems=None) -> tuple[Setup, dict, dict]:
     """-> (the fastest set-up, Engine keyword options, report).  systems:
     (system_of_particle, cylinders, wet) for batched beds, else None."""

@@ -1360,18 +1360,23 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   a.theta_seed = c->theta_seed;
   a.theta_max = c->theta_max;
   a.gate = c->step_gate;
-  /* threads per block: the option (a multiple of 32 up to 128), else 128 */
-  const int ob = c->opt.block_size;
-  const int bs = (ob >= 32 && ob <= 32 * kWarps && ob % 32 == 0) ? ob : 32 * kWarps;
   const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;
   if (net && !c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
+  const bool thread_loop = c->opt.pair_mode == DEM_PAIRS_THREAD || (c->opt.pair_mode == DEM_PAIRS_AUTO && net);
+  /* threads per block: the option (a multiple of 32 up to 128), else the
+   * fastest measured on the 200k wet bed: one warp for the warp-cooperative
+   * loop (a block frees its slot as soon as its only warp is done; 75.0 vs
+   * 79.5 us at 128 threads), two for the thread loop with the formula (81.5
+   * vs 83.5 us), four with the learned closure, whose weights are staged
+   * once per block */
+  const int ob = c->opt.block_size;
+  const int bs = (ob >= 32 && ob <= 32 * kWarps && ob % 32 == 0) ? ob : net ? 32 * kWarps : thread_loop ? 64 : 32;
   const int g = grid_for(c->n, bs);
   if (c->moving_walls) {
     k_move_walls<<<1, 32, 0, s>>>(b.cyl, b.n_sys > 0 ? b.n_sys : 1, c->s.prm.dt, c->step_gate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_check(e, "mixed_step wall motion");
   }
-  const bool thread_loop = c->opt.pair_mode == DEM_PAIRS_THREAD || (c->opt.pair_mode == DEM_PAIRS_AUTO && net);
   if (thread_loop) {
     if (net) k_step_mixed<true, true><<<g, bs, kCapSmem, s>>>(a);
     else if (c->s.force_cap == 1) k_step_mixed<true, false><<<g, bs, 0, s>>>(a);
