@@ -112,6 +112,32 @@ def test_pair_loops_agree(cuda, make):
     b.close()
 
 
+@pytest.mark.parametrize("pairs, sizes", [("warp", (32, 64, 96, 128)), ("thread", (32, 64, 128))])
+def test_block_size_does_not_change_results(cuda, pairs, sizes):
+    """The step kernel's block size (the default, 32 for the warp loop and 64
+    for the thread loop, or the option) only changes which warps share a
+    block: every warp's particles and arithmetic are the same, so 60 steps
+    with rebuilds give the same bits at every size."""
+    w = _workloads.small_wet()
+    pos, vel, ang = _workloads.stirred(w)
+    out = {}
+    for bs in (0,) + tuple(sizes):
+        e = Engine(w.setup, precision="mixed", pairs=pairs, block_size=bs)
+        e.set_state(pos, vel, ang)
+        e.step(60)
+        e.sync()
+        out[bs] = (e.get_state(), e.stats()["rebuilds"], e.history(_lockstep.max_per(w)))
+        e.close()
+    s0, r0, h0 = out[0]
+    assert r0 >= 1
+    for bs in sizes:
+        s, r, h = out[bs]
+        assert r == r0, bs
+        for k in ("pos", "vel", "angvel", "force"):
+            assert np.array_equal(s[k], s0[k]), (bs, k)
+        assert np.array_equal(h[0], h0[0]) and np.array_equal(h[1], h0[1]), bs
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_graph_replay_equals_host_stepping(cuda, precision):
     w = _workloads.small_wet()
