@@ -203,7 +203,7 @@ __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* _
                                 const int* __restrict__ nebor_idx, LevelView lv, double3 origin,
                                 double search_gap, int* __restrict__ nebor,
                                 int* __restrict__ num_nebor, int n, int* __restrict__ err, Prefilter pre) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = reversed_block_thread(); /* the largest spheres' long searches first */
   if (i >= n) return;
   const double3 o = pos[i];
   const double ri = rad[i];

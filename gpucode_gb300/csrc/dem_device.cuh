@@ -30,6 +30,16 @@ __device__ __forceinline__ double3 cross3(double3 a, double3 b) {
   return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 
+/* This thread's particle with the blocks taken in reverse.  Particles sit in
+ * level-major cell order, so the largest spheres -- the most neighbours, the
+ * longest loops -- come last; the GPU starts blocks roughly in index order,
+ * and in index order their blocks would run in the grid's tail.  Taken first,
+ * they overlap the many light blocks instead (each particle's work is its
+ * own, so the results are the same bits). */
+__device__ __forceinline__ int reversed_block_thread() {
+  return (int)((gridDim.x - 1 - blockIdx.x) * blockDim.x + threadIdx.x);
+}
+
 /* ---- cell hash (kernel.cu:617-641) ---- */
 __device__ __forceinline__ int3 grid_pos(double3 p, int lvl, const LevelView& lv, double3 origin) {
   const double cs = lv.cell_size[lvl];

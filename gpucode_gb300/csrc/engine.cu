@@ -70,7 +70,7 @@ __global__ void k_copy_old(const int* __restrict__ nebor, const int* __restrict_
                            ContactRec* __restrict__ rec_old, unsigned char* __restrict__ brg_old,
                            int* __restrict__ wlist_old, int* __restrict__ nwall_old,
                            ContactRec* __restrict__ wrec_old, int n, unsigned long long* counters) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = reversed_block_thread(); /* the longest slot lists first */
   if (p == 0 && counters) counters[4] += 1; /* rebuilds */
   if (p >= n) return;
   const int L = plevel[p];
@@ -157,7 +157,7 @@ __global__ void k_carry(const int* __restrict__ nebor, const int* __restrict__ n
                         const int* __restrict__ wlist_old, const int* __restrict__ nwall_old,
                         const ContactRec* __restrict__ wrec_old, ContactRec* __restrict__ wrec,
                         const int* __restrict__ src, const int* __restrict__ old_to_new, int n) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = reversed_block_thread(); /* the longest slot lists first */
   if (q >= n) return;
   const int p = src ? src[q] : q;
   const int L = plevel[q];

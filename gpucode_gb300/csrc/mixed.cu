@@ -576,7 +576,7 @@ __device__ __forceinline__ void finish_particle(const MixArgs& a, int q, int qq,
 template <bool WET, bool NET>
 __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArgs a) {
   if (a.n <= 0 || (a.gate && *a.gate)) return;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = reversed_block_thread(); /* the heaviest particles first */
   const bool live = q < a.n;
   const int qq = live ? q : a.n - 1;
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -988,7 +988,7 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = reversed_block_thread(); /* the heaviest particles first */
   const bool live = q < a.n;
   const int qq = live ? q : a.n - 1;
   extern __shared__ __align__(16) unsigned char dsm[];
