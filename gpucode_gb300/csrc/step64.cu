@@ -49,7 +49,9 @@ __global__ void __launch_bounds__(128) k_pp_force64(
     const int* __restrict__ lqd_old, double3* __restrict__ force, double3* __restrict__ mom,
     double* __restrict__ rmom, int n, int force_cap, int stage, DevConsts k,
     unsigned long long* __restrict__ counters) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  /* blocks in reverse: in cell order the largest spheres, with the most
+   * pairs, come last (in the reference's order this is only another schedule) */
+  const int i = reversed_block_thread();
   if (i >= n) return;
   LawCfg64 cfg;
   cfg.cal = &k.cal;
