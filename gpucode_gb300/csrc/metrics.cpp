@@ -1,8 +1,8 @@
 /*
  * metrics.cpp -- packing fraction and mean coordination number of a bed.
  *
- * The reference computes neither; these are the quantities the packing is
- * judged on.  Definitions:
+ * The reference computes neither; these are the quantities a packing's
+ * accuracy is stated in (against an all-FP64 run).  Definitions:
  *  - probe: the cylinder coaxial with the container, radius R - 3 d_max, from
  *    3 d_max above the floor to 3 d_max below the free surface; the free
  *    surface is the 98th percentile of the sphere tops (a few particles
