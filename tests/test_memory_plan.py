@@ -17,6 +17,7 @@ def test_estimate_adds_up():
     m = w.setup.memory("mixed")
     assert m["slots"] == s.n_pp_slots
     assert m["per_slot"] == 138 and m["per_particle"] == 752 + 144
+    assert m["per_cell"] == 12  # cell start, end and offset
     low = m["per_particle"] * s.np + m["per_slot"] * s.n_pp_slots + m["per_cell"] * s.sys_ncells
     assert low < m["total"] < low + 200 * 2 ** 20
     assert w.setup.memory("fp64")["per_particle"] == 752
