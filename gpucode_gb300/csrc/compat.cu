@@ -379,27 +379,18 @@ namespace {
 constexpr size_t kStaticSortScratchBytes = size_t(16) << 20;
 static __device__ __align__(256) unsigned char g_static_sort_scratch[kStaticSortScratchBytes];
 
-/* its address on each device, looked up once per device */
-constexpr int kMaxStaticDevices = 64;
-std::mutex g_static_mu;
-void* g_static_scratch_at[kMaxStaticDevices] = {};
-
+/* The array's device address in the current context, looked up on every call:
+ * the lookup is a table read once the library's device code is loaded, and a
+ * cached address would go stale when the caller resets the device
+ * (cudaDeviceReset) or a new primary context loads the code elsewhere.  The
+ * name g_static_sort_scratch is a host-side stand-in in host code: only this
+ * address may be handed to kernels. */
 dem_status static_scratch(void** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return dem::cuda_check(e, "BldNeborListNoAlloc: cudaGetDevice");
-  if (dev < 0 || dev >= kMaxStaticDevices)
-    return dem::fail(DEM_ERR_ARG, "BldNeborListNoAlloc: device index " + std::to_string(dev) +
-                                      " is beyond the " + std::to_string(kMaxStaticDevices) + " it tracks");
-  std::lock_guard<std::mutex> lock(g_static_mu);
-  if (!g_static_scratch_at[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_static_sort_scratch);
-    if (e != cudaSuccess) return dem::cuda_check(e, "BldNeborListNoAlloc: cudaGetSymbolAddress");
-    if (!p) return dem::fail(DEM_ERR_CUDA, "BldNeborListNoAlloc: the static scratch has no device address");
-    g_static_scratch_at[dev] = p;
-  }
-  *out = g_static_scratch_at[dev];
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_static_sort_scratch);
+  if (e != cudaSuccess) return dem::cuda_check(e, "BldNeborListNoAlloc: cudaGetSymbolAddress");
+  if (!p) return dem::fail(DEM_ERR_CUDA, "BldNeborListNoAlloc: the static scratch has no device address");
+  *out = p;
   return DEM_OK;
 }
 

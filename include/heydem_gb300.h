@@ -34,6 +34,12 @@
 #include <stdio.h>
 #include <vector_types.h> /* double2, double3, int3: layout of the reference's structs */
 
+/* The reference's heydem.h defines `gravity` as a macro (heydem.h:16); a
+ * translation unit that includes it first still sees this header's field of
+ * that name as a field.  The macro is back in force after this header. */
+#pragma push_macro("gravity")
+#undef gravity
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -405,9 +411,15 @@ int dem_compat_errors(void);
  * cell sort's scratch is a fixed 16 MiB array of device memory inside the
  * library: 4 * (2 * TotalParticle + ceil(Sys_nCells / 2048) + 64) bytes must
  * fit, i.e. up to about 2,000,000 particles; larger sizes return DEM_ERR_ARG
- * with a message and launch nothing.  The first call on each device looks the
- * array's address up (make it before any stream capture).  Calls share that
- * one array: two calls whose kernels run at the same time on one device race.
+ * with a message and launch nothing.  Every call looks the array's address
+ * up in the current context (cudaGetSymbolAddress), so the call stays valid
+ * after cudaDeviceReset.  With CUDA's lazy module loading (the default), the
+ * array is committed when the library's device code first loads on a device,
+ * which can be this call's first use: a caller that reserves the rest of the
+ * card's memory up front should make one call (or run with
+ * CUDA_MODULE_LOADING=EAGER) before reserving, and make that first call
+ * before any stream capture.  Calls share that one array: two calls whose
+ * kernels run at the same time on one device race.
  * Returns DEM_OK or a negative dem_status (see dem_last_error). */
 int BldNeborListNoAlloc(int* d_GridParticleHash, int* d_GridParticleIndex, int* d_CellStart,
                         int* d_CellEnd, int* d_pLevel, SEARCHCELL d_cell, int* d_Ncell_Idx,
@@ -543,4 +555,5 @@ const char* dem_version(void);
 #ifdef __cplusplus
 }
 #endif
+#pragma pop_macro("gravity")
 #endif /* HEYDEM_GB300_H */

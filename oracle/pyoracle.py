@@ -5,6 +5,7 @@ bench.py's CPU-baseline leg use it, as the checker or the timed CPU baseline."""
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -17,7 +18,17 @@ ROOT = Path(__file__).resolve().parents[1]  # repository root
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "libdem_oracle.so"
 REF_LIB = ORACLE_DIR / "_ref" / "libdem_ref.so"
-REF_SRC = Path("/root/reference")
+
+
+def reference_dir() -> Path:
+    """The reference's source tree: $DEM_REF_DIR when set, else the tree checked out
+    beside this repository (../reference).  It may be absent (then only the oracle
+    and the golden fixtures are available)."""
+    env = os.environ.get("DEM_REF_DIR")
+    return Path(env) if env else ROOT.parent / "reference"
+
+
+REF_SRC = reference_dir()
 
 
 class OConsts(C.Structure):
@@ -65,7 +76,7 @@ def ref_available() -> bool:
     if REF_LIB.exists():
         return True
     if (REF_SRC / "kernel.cu").exists():
-        r = subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref"], capture_output=True)
+        r = subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF_DIR={REF_SRC}"], capture_output=True)
         return r.returncode == 0 and REF_LIB.exists()
     return False
 
@@ -165,50 +176,50 @@ class OracleSim:
             acc += s.level_nnebors[l] * s.level_npars[l]
         return base
 
+    def lists_flat(self) -> tuple[np.ndarray, np.ndarray]:
+        """(counts, every particle's partners end to end: particle-major, list order)."""
+        num = self.arr("Num_Nebor", np.int32, self.n).copy()
+        _, _, sl = self.slots_of(num)
+        return num, self.arr("Nebor1", np.int32, self.slots)[sl].copy()
+
     def lists(self) -> tuple[np.ndarray, list[np.ndarray]]:
         """(counts, per-particle partner arrays in list order)."""
-        num = self.arr("Num_Nebor", np.int32, self.n).copy()
-        neb = self.arr("Nebor1", np.int32, self.slots)
-        base = self.slot_base()
-        npars = np.array(list(self.setup.s.level_npars)[: self.setup.s.n_levels], np.int64)
-        out = []
-        for i in range(self.n):
-            L = self.setup.plevel[i]
-            idx = base[L] + np.arange(num[i]) * npars[L] + self.setup.nidx[i]
-            out.append(neb[idx].copy())
-        return num, out
+        num, flat = self.lists_flat()
+        return num, np.split(flat, np.cumsum(num)[:-1]) if self.n else []
 
-    def history(self) -> list[np.ndarray]:
-        """per-particle (count, 8) records: dispt xyz, nDsp, nDsp_mx, plstRad, plstDfm, stage; plus lqdBrg."""
+    def history_flat(self) -> np.ndarray:
+        """(used slots, 9) records, particle-major in list order: dispt xyz, nDsp,
+        nDsp_mx, plstRad, plstDfm, stage, lqdBrg."""
         num = self.arr("Num_Nebor", np.int32, self.n)
-        base = self.slot_base()
-        s = self.setup.s
-        npars = np.array(list(s.level_npars)[: s.n_levels], np.int64)
+        _, _, idx = self.slots_of(num)
         f = {k: self.arr("pp." + k, np.float64, self.slots) for k in ("nDsp", "nDsp_mx", "plstRad", "plstDfm")}
         disp = self.arr("pp.dispt", np.float64, 3 * self.slots).reshape(-1, 3)
         stage = self.arr("pp.stage", np.int32, self.slots)
         brg = self.arr("pp.lqdBrg", np.int32, self.slots)
-        out = []
-        for i in range(self.n):
-            L = self.setup.plevel[i]
-            idx = base[L] + np.arange(num[i]) * npars[L] + self.setup.nidx[i]
-            rec = np.column_stack([disp[idx], f["nDsp"][idx], f["nDsp_mx"][idx], f["plstRad"][idx],
-                                   f["plstDfm"][idx], stage[idx].astype(np.float64), brg[idx].astype(np.float64)])
-            out.append(rec)
-        return out
+        return np.column_stack([disp[idx], f["nDsp"][idx], f["nDsp_mx"][idx], f["plstRad"][idx],
+                                f["plstDfm"][idx], stage[idx].astype(np.float64), brg[idx].astype(np.float64)])
+
+    def history(self) -> list[np.ndarray]:
+        """per-particle (count, 9) records: dispt xyz, nDsp, nDsp_mx, plstRad, plstDfm, stage; plus lqdBrg."""
+        num = self.arr("Num_Nebor", np.int32, self.n)
+        return np.split(self.history_flat(), np.cumsum(num)[:-1]) if self.n else []
 
     def slots_of(self, counts: np.ndarray) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """(particle, list position, slot) of every used neighbour slot."""
         s = self.setup.s
         base = self.slot_base()
         npars = np.array(list(s.level_npars)[: s.n_levels], np.int64)
+        counts = np.asarray(counts, np.int64)
         ii = np.repeat(np.arange(self.n), counts)
-        kk = np.concatenate([np.arange(c) for c in counts]) if len(counts) else np.zeros(0, np.int64)
+        start = np.cumsum(counts) - counts
+        kk = np.arange(len(ii), dtype=np.int64) - np.repeat(start, counts)
         L = self.setup.plevel[ii]
         return ii, kk, base[L] + kk * npars[L] + self.setup.nidx[ii]
 
     def load_state(self, pos, vel, angvel, pmove, lqd, counts, partners, rec, brg, nwall, wlist, wrec, flag, it):
-        """Resume from another implementation's full state (reference layouts)."""
+        """Resume from another implementation's full state (reference layouts).
+        partners, rec (8 columns) and brg hold the used slots end to end,
+        particle-major in list order (the order of slots_of)."""
         n = self.n
         self.vec("pos")[:] = pos
         self.vec("vel")[:] = vel
@@ -216,14 +227,14 @@ class OracleSim:
         self.arr("pMove", np.float64, n)[:] = pmove
         self.arr("lqdCnt", np.int32, n)[:] = lqd
         self.arr("Num_Nebor", np.int32, n)[:] = counts
-        ii, kk, sl = self.slots_of(counts)
-        self.arr("Nebor1", np.int32, self.slots)[sl] = partners[ii, kk]
-        r = rec[ii, kk]
+        _, _, sl = self.slots_of(counts)
+        self.arr("Nebor1", np.int32, self.slots)[sl] = partners
+        r = np.asarray(rec).reshape(-1, 8)
         self.arr("pp.dispt", np.float64, 3 * self.slots).reshape(-1, 3)[sl] = r[:, 0:3]
         for c, f in enumerate(("nDsp", "nDsp_mx", "plstRad", "plstDfm")):
             self.arr("pp." + f, np.float64, self.slots)[sl] = r[:, 3 + c]
         self.arr("pp.stage", np.int32, self.slots)[sl] = r[:, 7].astype(np.int32)
-        self.arr("pp.lqdBrg", np.int32, self.slots)[sl] = brg[ii, kk]
+        self.arr("pp.lqdBrg", np.int32, self.slots)[sl] = brg
         self.arr("nwall", np.int32, n)[:] = nwall
         self.arr("wlist", np.int32, 3 * n)[:] = np.asarray(wlist).reshape(-1)
         wr = np.asarray(wrec).reshape(n, 3, 8)

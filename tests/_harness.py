@@ -7,5 +7,5 @@ if str(_ORACLE) not in sys.path:
     sys.path.insert(0, str(_ORACLE))
 
 from pyoracle import *  # noqa: E402,F401,F403
-from pyoracle import (ORACLE_DIR, ORACLE_LIB, REF_LIB, OracleSim, build_oracle, consts_of, oracle,  # noqa: E402,F401
+from pyoracle import (ORACLE_DIR, ORACLE_LIB, REF_LIB, REF_SRC, OracleSim, build_oracle, consts_of, oracle,  # noqa: E402,F401
                       ref, ref_available, sim_arrays)

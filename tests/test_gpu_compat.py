@@ -154,22 +154,18 @@ FP64_TOL = {"force": 1e-12, "pos": 1e-14, "vel": 1e-12, "hist": 1e-12}
 
 
 def _snap(drv, sim, w):
-    """the driver's device state (reference layouts) in the lockstep comparison's terms"""
+    """the driver's device state (reference layouts) in the lockstep comparison's
+    terms: lists and contact records as the used slots end to end"""
     g = lambda x: x.detach().cpu().numpy()  # noqa: E731
     n = drv.n
-    mp = _lockstep.max_per(w)
     num = g(drv.num)
-    ii, kk, sl = sim.slots_of(num)
-    partners = np.full((n, mp), -1, np.int32)
-    partners[ii, kk] = g(drv.neb)[sl]
+    _, _, sl = sim.slots_of(num)
     pp = {k: g(v) for k, v in drv.pp[0].items()}
-    rec = np.zeros((n, mp, 8))
-    rec[ii, kk, 0:3] = pp["dispt"][sl]
+    rec = np.zeros((len(sl), 8))
+    rec[:, 0:3] = pp["dispt"][sl]
     for c, f in enumerate(("nDsp", "nDsp_mx", "plstRad", "plstDfm")):
-        rec[ii, kk, 3 + c] = pp[f][sl]
-    rec[ii, kk, 7] = pp["stage"][sl]
-    brg = np.zeros((n, mp), np.int32)
-    brg[ii, kk] = pp["lqdBrg"][sl]
+        rec[:, 3 + c] = pp[f][sl]
+    rec[:, 7] = pp["stage"][sl]
     pw = {k: g(v) for k, v in drv.pw[0].items()}
     wrec = np.zeros((n, 3, 8))
     for a in range(3):
@@ -179,8 +175,8 @@ def _snap(drv, sim, w):
             wrec[:, a, 3 + c] = pw[f][rows]
         wrec[:, a, 7] = pw["stage"][rows]
     return dict(pos=g(drv.pos), vel=g(drv.vel), angvel=g(drv.ang), force=g(drv.force), pmove=g(drv.pmove),
-                lqd=g(drv.lqd), counts=num, partners=partners, rec=rec, brg=brg, nwall=g(drv.nw), wlist=g(drv.wl),
-                wrec=wrec, flag=int(drv.flag.item()))
+                lqd=g(drv.lqd), counts=num, partners=g(drv.neb)[sl], rec=rec, brg=pp["lqdBrg"][sl],
+                nwall=g(drv.nw), wlist=g(drv.wl), wrec=wrec, flag=int(drv.flag.item()))
 
 
 def _load_oracle_from(drv, sim):

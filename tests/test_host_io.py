@@ -47,7 +47,7 @@ def test_files_roundtrip_equals_direct_setup(in_tmp, k):
 @pytest.mark.parametrize("k", [0, 1, 2])
 def test_setup_equals_reference_readdata(in_tmp, k):
     if not _harness.ref_available():
-        pytest.skip("reference sources not present")
+        pytest.skip(f"reference sources not found at {_harness.REF_SRC} (set DEM_REF_DIR)")
     w = _cases()[k]
     configs.write_heyi("heyi", w.inp, w.dia)
     mine = Setup.from_files("heyi")
@@ -147,7 +147,7 @@ def test_diameter_list_tiles_and_ignores_trailing_whitespace(in_tmp):
 
 def test_wrtec_matches_reference_byte_for_byte(in_tmp):
     if not _harness.ref_available():
-        pytest.skip("reference sources not present")
+        pytest.skip(f"reference sources not found at {_harness.REF_SRC} (set DEM_REF_DIR)")
     lib = _abi.load()
     ref = _harness.ref()
     rng = np.random.Generator(np.random.PCG64(5))

@@ -17,7 +17,8 @@ import _workloads
 @pytest.fixture(scope="module")
 def have_ref():
     if not _harness.ref_available():
-        pytest.skip("reference sources not present: pinned by tests/golden instead")
+        pytest.skip(f"reference sources not found at {_harness.REF_SRC} (set DEM_REF_DIR): pinned by "
+                    "tests/golden instead")
 
 
 def _run_pair(w, steps, check_every):
