@@ -2,13 +2,21 @@
 """Benchmark: particle-steps/s of the wet polydisperse packing (200,000 spheres)
 on one GB300, FP32-force / FP64-state path.
 
+The bed is tests/golden/packed_wet200k.npz: the wet workload's 200,000
+log-normal spheres (median 1 mm, sigma_ln 0.2 in [0.5, 2] mm, cylinder R =
+25 mm, capillary bridges, dt 5e-7 s) packed to a packing fraction of 0.662 and
+a mean coordination number of 6.6 (tests/golden/make_packed_bed.py), at rest,
+contact histories empty.  Both arms read it from the file: --impl reference
+runs the FP64 oracle (the reference's algorithm on the host cores) and never
+loads the GPU library.  Each arm takes --warmup steps from the bed (the first
+builds the neighbour lists), then times --steps steps.
+
 One bench "step" is one DEM time step of the whole bed (rebuild when flagged,
 p-p contact + capillary, wall contact, integration), replayed from a one-step
 CUDA graph whose rebuild decision is taken on the device.  The working set of a
-step (~90 MB) fits in the 129 MB L2, so L2 is evicted between timed steps (a
-256 MB write followed by a 256 MB read on the same stream, outside the per-step
-CUDA events, so the step starts cold and pays no write-backs of the eviction).
-Before timing, the deposited bed settles under gravity for --settle steps.
+step (~210 MB) is larger than the 129 MB L2; L2 is evicted between timed steps
+all the same (a 256 MB write followed by a 256 MB read on the same stream,
+outside the per-step CUDA events).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -35,6 +43,15 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "particle-steps/s, 200k wet spheres, vs FP64 plain; packing-frac & Z error"
 UNIT = "particle-steps/s"
+BED = ROOT / "tests" / "golden" / "packed_wet200k.npz"
+DATA = "synthetic (seeded log-normal sizes, packed bed from tests/golden/packed_wet200k.npz)"
+
+
+def bed_config(w) -> dict:
+    """the workload both arms time (identical in both lines)"""
+    return {"workload": "wet200k-packed", "particles": w.setup.n, "levels": int(w.setup.s.n_levels), "dt_s": 5e-7,
+            "bed": "tests/golden/packed_wet200k.npz (phi 0.662, Z 6.6; at rest, empty histories)",
+            "start": "warm-up steps from the bed (the first builds the lists), then the timed steps"}
 
 
 def _peaks() -> tuple[float, str]:
@@ -142,11 +159,14 @@ def cpu_oracle_rate(w, pos, steps: int, threads: int) -> tuple[float, str]:
 
 
 def run_reference(args, ws, rank):
+    """The reference's algorithm (the FP64 oracle restating kernel.cu and the
+    main.cpp step) on the host cores, on the same bed file as the GPU arm; the
+    GPU library is not loaded."""
     if rank != 0:
         return
     from gpucode_gb300 import configs
 
-    w = configs.wet()
+    w = configs.load_bed(BED)
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -155,7 +175,7 @@ def run_reference(args, ws, rank):
     if not pyoracle.ORACLE_LIB.exists():
         pyoracle.build_oracle()
     sim = pyoracle.OracleSim(w.setup, w.pos0_reduced)
-    sim.step(1 + args.warmup)
+    sim.step(args.warmup)
     t0 = time.perf_counter()
     sim.step(args.steps)
     dt = time.perf_counter() - t0
@@ -163,11 +183,11 @@ def run_reference(args, ws, rank):
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded deposited bed, log-normal sizes)",
-        "config": {"workload": "wet200k", "particles": w.setup.n, "dt_s": 5e-7, "levels": int(w.setup.s.n_levels)},
+        "vs_baseline": None, "dtype": "f64", "data": DATA, "config": bed_config(w),
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} steps of the full bed on the host cores (FP64 oracle restating "
-                                   "the reference kernels; the reference sources are not on this host)"},
+                         "sample": f"{args.steps} steps of the full bed after {args.warmup} warm-up steps, on the "
+                                   "host cores (FP64 oracle restating the reference kernels; the reference sources "
+                                   "are not on this host)"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -497,7 +517,7 @@ def run_wet_large(args, which: str):
         m = packing_metrics(w.setup, e.get_state()["pos"])
         r = {"particle_steps_per_s": ps / dt, "wall_s": dt, "rebuilds": s1["rebuilds"] - s0["rebuilds"],
              "clocks": ck, "per_step_counts": cnt, "phi": m["phi"], "z": m["z"], "n_probe": m["n_probe"],
-             "roofline": {"kernel": step_kernel("auto", cap), "kernel_ms": ms_k.value, "bytes_per_particle": bpp,
+             "roofline": {"kernel": e.step_kernel_name(), "kernel_ms": ms_k.value, "bytes_per_particle": bpp,
                           "achieved": ach, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                           "frac": ach / peak, "l2": "working set far above L2 (no eviction needed)"}}
         if cap == "formula":
@@ -576,12 +596,6 @@ def kernel_table(e, n: int) -> list:
     return rows
 
 
-def step_kernel(pairs: str, capillary: str = "formula") -> str:
-    """the step kernel the library launches for this pair loop and closure"""
-    thread = pairs == "thread" or (pairs == "auto" and capillary == "mlp")
-    return ("k_step_mixed" if thread else "k_step_coop") + ("<1,1>" if capillary == "mlp" else "<1,0>")
-
-
 def traffic_from_profiles(kernel: str) -> float | None:
     """DRAM bytes per launch of the fused step kernel from the committed ncu summary."""
     name = "step_mixed_wet200k.md" if kernel.startswith("k_step_mixed") else "step_coop_wet200k.md"
@@ -606,27 +620,29 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--profile-reps", type=int, default=20)
-    ap.add_argument("--settle", type=int, default=2000,
-                    help="untimed steps before the warm-up: gravity loads the deposited bed's contacts")
-    ap.add_argument("--no-fp64-check", dest="fp64_check", action="store_false",
-                    help="skip the FP64 rerun that gives the packing-fraction and coordination errors")
+    ap.add_argument("--accuracy-steps", type=int, default=2000,
+                    help="steps of the mixed and FP64 engines from the bed for the packing-fraction / Z errors "
+                         "(0: skip)")
+    ap.add_argument("--oracle-steps", type=int, default=300,
+                    help="steps of the CPU oracle from the bed, compared with both engines (0: skip)")
     ap.add_argument("--capnet-samples", type=int, default=5_000_000,
-                    help="training samples for the learned capillary closure, logged while settling (0: skip it)")
+                    help="training samples for the learned capillary closure, logged from the bed (0: skip it)")
     ap.add_argument("--capnet-epochs", type=int, default=20)
+    ap.add_argument("--sample-steps", type=int, default=2000,
+                    help="steps of the bed over which the closure's training samples are logged")
     ap.add_argument("--ref-gpu-steps", type=int, default=40,
                     help="timed steps of the reference's own kernels on this GPU (0: skip)")
     ap.add_argument("--host-steps", action="store_true",
-                    help="launch every step's kernels directly instead of from CUDA graphs (for ncu, which "
-                         "cannot profile kernels of graphs with conditional nodes)")
+                    help="launch every step's kernels directly instead of from CUDA graphs")
     ap.add_argument("--workload", default="wet200k",
                     choices=["wet200k", "wet200k-full", "dry5k", "ensemble", "wet2m", "wet16m"],
-                    help="wet200k: the headline bench; wet200k-full: the wet bed's whole run, FP64 against the "
-                         "fast paths; dry5k: the dry lattice packing run whole on GPU and CPU; ensemble: "
-                         "independent packings batched in one engine; wet2m / wet16m: large wet beds with the "
-                         "fused learned closure")
+                    help="wet200k: the headline bench on the packed bed; wet200k-full: the wet deposit's whole "
+                         "run, FP64 against the fast paths; dry5k: the dry lattice packing run whole on GPU and "
+                         "CPU; ensemble: independent packings batched in one engine; wet2m / wet16m: large wet "
+                         "beds with the fused learned closure")
     ap.add_argument("--pairs", default="auto", choices=["auto", "warp", "thread"],
                     help="pair loop of the step kernel: warp-cooperative, one thread per particle, or auto (the "
-                         "library's default: warp with the capillary formula, thread with the learned closure)")
+                         "library's choice)")
     ap.add_argument("--block-size", type=int, default=0, help="threads per block of the step kernel (0: default)")
     ap.add_argument("--full-steps", type=int, default=50000)
     ap.add_argument("--large-steps", type=int, default=0, help="steps of wet2m / wet16m (0: 10,000 / 5,000)")
@@ -656,6 +672,11 @@ def main():
         if rank == 0:
             run_wet_large(args, args.workload)
         return
+    run_headline(args, ws, rank)
+
+
+def run_headline(args, ws, rank):
+    import ctypes as C
 
     import torch
 
@@ -667,18 +688,16 @@ def main():
         dist.init_process_group("nccl", init_method="env://")
 
     from gpucode_gb300 import configs
-    from gpucode_gb300.engine import Engine
-
-    w = configs.wet()
-    n = w.setup.n
-    import ctypes as C
-
     from gpucode_gb300._abi import check, ptr
+    from gpucode_gb300.engine import Engine, packing_metrics
+
+    w = configs.load_bed(BED)
+    n = w.setup.n
+    pos0 = w.pos0_reduced
 
     eng = Engine(w.setup, precision="mixed", use_graph=not args.host_steps, graph_steps=1, pairs=args.pairs,
                  block_size=args.block_size)
-    eng.set_state(w.pos0_reduced)
-    stream = torch.cuda.ExternalStream(eng.stream())
+    eng.set_state(pos0)
     # L2 eviction between timed steps: write 256 MB, then read another 256 MB,
     # so each step starts with a cold L2 holding clean, unrelated lines
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
@@ -719,35 +738,14 @@ def main():
         e.sync()
         return sum(a.elapsed_time(b) for a, b in evs), wall, ckk, before, e.stats()
 
-    # settle; the learned closure's training samples are logged from the formula
-    # engine along the way (outside every timed region)
-    from gpucode_gb300 import capnet as cn
-
-    use_net = rank == 0 and args.capnet_samples > 0 and not args.host_steps
-    n_snap = 11
-    per_snap = -(-args.capnet_samples // n_snap)
-    xs, ys = [], []
-    if use_net and args.settle >= 2 * n_snap:
-        first = args.settle - n_snap * (args.settle // (n_snap + 1))
-        eng.step(first)
-        for _ in range(n_snap):
-            eng.step(args.settle // (n_snap + 1))
-            x, y = cn.collect_samples(eng, per_snap)
-            xs.append(x.clone())
-            ys.append(y.clone())
-    else:
-        eng.step(args.settle)
     eng.step(args.warmup)
     ms, t_wall, ck, s0, s1 = timed_steps(eng, args.steps)
-    steps_run = args.settle + args.warmup + args.steps
-    pos_mixed = eng.get_state()["pos"]
-    steps = args.steps
-    value, t_slow = replica_rate(ms / 1000.0, n, steps, ws)
+    value, t_slow = replica_rate(ms / 1000.0, n, args.steps, ws)
     ms = 1000.0 * t_slow
 
     # measured pair counts per particle-step over the timed region
     d = {k: s1[k] - s0[k] for k in ("nb_entries", "contacts", "bridges", "wall_contacts", "rebuilds")}
-    ps = n * steps
+    ps = n * args.steps
     n_nb, n_c, n_w, n_wall = d["nb_entries"] / ps, d["contacts"] / ps, d["bridges"] / ps, d["wall_contacts"] / ps
     bytes_per_particle = 152 + 4 * n_nb + 128 * n_c + 16 * n_w + 128 * n_wall
 
@@ -757,137 +755,37 @@ def main():
                                    C.byref(ms_k)), "dem_profile_step")
     peak, peak_kind = _peaks()
     achieved = n * bytes_per_particle / (ms_k.value * 1e-3) / 1e9
-    kname = step_kernel(args.pairs)
+    kname = eng.step_kernel_name()
     traffic = traffic_from_profiles(kname)
+    rebuild = rebuild_cost(eng, n)
 
     # end to end through the public API with host buffers: H2D state, one step, D2H state + force
-    hp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
-    hv = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
-    hw = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
-    hf = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
-    check(eng.lib.dem_get_state(eng.h, ptr(hp), ptr(hv), ptr(hw), None, None), "dem_get_state")
-    E = args.e2e_steps
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(E):
-        check(eng.lib.dem_set_state_ex(eng.h, ptr(hp), ptr(hv), ptr(hw), 0), "dem_set_state_ex")
-        check(eng.lib.dem_step(eng.h, 1), "dem_step")
-        check(eng.lib.dem_get_state(eng.h, ptr(hp), ptr(hv), ptr(hw), ptr(hf), None), "dem_get_state")
-    e2e_t = time.perf_counter() - t0
-    e2e, e2e_t = replica_rate(e2e_t, n, E, ws)
+    e2e, e2e_parts = end_to_end(eng, n, args.e2e_steps, ws)
     eng.sync()
 
-    # accuracy: the same bed, the same number of steps, all-FP64 reference formulas
+    # accuracy against FP64 runs of the reference's formulas from the same bed:
+    # this library's FP64 engine (pinned to the oracle step by step) over a long
+    # window, and the CPU oracle itself over a shorter one
     accuracy = None
-    mr = None
-    from gpucode_gb300.engine import packing_metrics
+    if rank == 0 and (args.accuracy_steps > 0 or args.oracle_steps > 0):
+        accuracy = accuracy_runs(w, args, torch)
 
-    if rank == 0 and args.fp64_check:
-        ref = Engine(w.setup, precision="fp64", use_graph=True)
-        ref.set_state(w.pos0_reduced)
-        t0 = time.perf_counter()
-        ref.step(steps_run)
-        ref.sync()
-        t_fp64 = time.perf_counter() - t0
-        pos_ref = ref.get_state()["pos"]
-        ref.close()
-        mm, mr = packing_metrics(w.setup, pos_mixed), packing_metrics(w.setup, pos_ref)
-        accuracy = {"steps_compared": steps_run, "phi_mixed": mm["phi"], "phi_fp64": mr["phi"],
-                    "phi_rel_err": abs(mm["phi"] - mr["phi"]) / mr["phi"], "z_mixed": mm["z"], "z_fp64": mr["z"],
-                    "z_rel_err": abs(mm["z"] - mr["z"]) / max(mr["z"], 1e-300), "n_probe": mr["n_probe"],
-                    "fp64_particle_steps_per_s": n * steps_run / t_fp64,
-                    "max_position_diff": float(np.abs(pos_mixed - pos_ref).max())}
-
-    # the learned capillary closure: trained on the logged samples by the
-    # library's own kernels, then the same bed stepped from the start with the
-    # network fused into the step kernel (BF16 tensor-core tiles)
+    # the learned capillary closure: samples of the plain formula logged from
+    # the bed, trained by the library's own kernels, then the same bed stepped
+    # with the network fused in the step kernel (BF16 tensor-core tiles)
     closure = None
-    if use_net and xs:
-        x = torch.cat(xs).contiguous()
-        y = torch.cat(ys).contiguous()
-        xs, ys = [], []
-        net = cn.CapNet(seed=0)
-        rep = net.fit(x, y, epochs=args.capnet_epochs, batch=8192, lr=1e-3, val_frac=0.1, seed=2024)
-        em = Engine(w.setup, precision="mixed", capillary="mlp", graph_steps=1, pairs=args.pairs,
-                    block_size=args.block_size)
-        em.set_capnet(net)
-        em.set_state(w.pos0_reduced)
-        em.step(args.settle + args.warmup)
-        ms_m, _, ck_m, m0, m1 = timed_steps(em, args.steps, all_ranks=False)
-        value_m = n * args.steps / (ms_m / 1000.0)
-        ms_km = C.c_double()
-        check(em.lib.dem_profile_step(em.h, args.profile_reps, C.c_void_p(flush.data_ptr()), flush.numel(),
-                                      C.byref(ms_km)), "dem_profile_step")
-        pos_m = em.get_state()["pos"]
-        evals, falls = m1["cap_mlp"] - m0["cap_mlp"], m1["cap_fallback"] - m0["cap_fallback"]
-        em.close()
-
-        def per_call_ms(fn, reps=5):
-            fn()
-            torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            for _ in range(reps):
-                fn()
-            b.record()
-            torch.cuda.synchronize()
-            return a.elapsed_time(b) / reps
-
-        big = x[: min(len(x), 2_000_000)].contiguous()
-        nb = len(big)
-        rates = {"network_bf16_tensor_cores": nb / per_call_ms(lambda: net.infer(big, True)) * 1e3,
-                 "network_fp32": nb / per_call_ms(lambda: net.infer(big, False)) * 1e3,
-                 "formula_fp64_as_reference": nb / per_call_ms(lambda: cn.formula(big, True)) * 1e3,
-                 "formula_fp32_step_kernel": nb / per_call_ms(lambda: cn.formula(big, False)) * 1e3}
-        net.close()
-        closure = {"value": value_m, "unit": UNIT, "ms_per_step": ms_m / args.steps, "kernel_ms": ms_km.value,
-                   "clocks": ck_m, "samples": len(x), "epochs": rep["epochs"], "fit_seconds": rep["seconds"],
-                   "val_mse_standardised": rep["val_mse"], "val_force_rel_err_mean": rep["val_force_rel_mean"],
-                   "val_force_rel_err_max": rep["val_force_rel_max"],
-                   "val_rupture_rel_err_max": rep["val_rupture_rel_max"],
-                   "rebuilds": m1["rebuilds"] - m0["rebuilds"],
-                   "network_evaluations_per_step": evals / args.steps,
-                   "formula_fallback_fraction": falls / max(evals + falls, 1),
-                   "evaluations_per_s": rates}
-        mmlp = packing_metrics(w.setup, pos_m)
-        closure["phi"] = mmlp["phi"]
-        closure["z"] = mmlp["z"]
-        if mr is not None:
-            closure["phi_rel_err_vs_fp64"] = abs(mmlp["phi"] - mr["phi"]) / mr["phi"]
-            closure["z_rel_err_vs_fp64"] = abs(mmlp["z"] - mr["z"]) / max(mr["z"], 1e-300)
-        del x, y, big
+    if rank == 0 and args.capnet_samples > 0 and not args.host_steps:
+        closure = learned_closure(w, args, timed_steps, torch, flush)
 
     # the reference's own kernels (kernel.cu built for sm_103a) on this GPU, same bed
     ref_gpu = None
     if rank == 0 and args.ref_gpu_steps > 0:
-        from baseline import refgpu
-
-        ok, why = refgpu.available()
-        if not ok:
-            ref_gpu = {"unavailable": why}
-        else:
-            stt = eng.get_state()
-            try:
-                r, _ = refgpu.run(w.setup, stt["pos"], stt["vel"], stt["angvel"], 5, args.ref_gpu_steps,
-                                  flush.data_ptr(), flush.numel())
-                rv = n / (r["step_ms"] * 1e-3)
-                ref_gpu = {"value": rv, "unit": UNIT, "ms_per_step": r["step_ms"],
-                           "kernel_ms": {"PPForceCalcG": r["force_ms"], "CirPWInterG": r["wall_ms"],
-                                         "UpdateSystemG": r["update_ms"]},
-                           "rebuilds": r["rebuilds"], "slot_overflow": bool(r["overflow"]),
-                           "speedup": value / rv,
-                           "speedup_with_learned_closure": closure["value"] / rv if closure else None,
-                           "kernel_speedup": (r["force_ms"] + r["wall_ms"] + r["update_ms"]) / ms_k.value,
-                           "sample": f"{args.ref_gpu_steps} steps after 5 warm-up from this bed's final state, "
-                                     "histories empty, L2 evicted before each step, main.cpp step order "
-                                     "(per-step flag read, VarInit memsets)"}
-            except RuntimeError as e:
-                ref_gpu = {"unavailable": str(e)}
+        ref_gpu = reference_kernels(w, args, flush, value, closure, ms_k.value)
 
     if rank == 0:
         threads = os.cpu_count() or 1
         if args.cpu_steps > 0:
-            cpu_val, cpu_sample = cpu_oracle_rate(w, w.pos0_reduced, args.cpu_steps, threads)
+            cpu_val, cpu_sample = cpu_oracle_rate(w, pos0, args.cpu_steps, threads)
         else:
             cpu_val, cpu_sample = None, "skipped (--cpu-steps 0)"
         launches_per_step = 2  # fused step kernel + k_chain (the chained one-step graph)
@@ -896,25 +794,25 @@ def main():
         # neighbour, wall list, carry), then the step again (counted in launches_per_step)
         rebuild_launches = 2 + 15
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": args.warmup,
-            "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32-force/f64-state", "data": "synthetic (seeded deposited bed, log-normal sizes)",
-            "config": {"workload": "wet200k", "particles": n, "levels": int(w.setup.s.n_levels), "dt_s": 5e-7,
-                       "capillary": "formula", "pair_loop": args.pairs,
-                       "parallelism": "replicas" if ws > 1 else "single",
-                       "l2": "evicted between timed steps (256 MB write + 256 MB read, outside the per-step events)",
-                       "per_step_counts": {"n_nb": n_nb, "n_c": n_c, "n_w": n_w, "n_wall": n_wall,
-                                           "rebuilds": d["rebuilds"]},
-                       "wall_s": t_wall},
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-force/f64-state", "data": DATA, "config": bed_config(w),
+            "run": {"capillary": "formula", "pair_loop": kname, "parallelism": "replicas" if ws > 1 else "single",
+                    "l2": "evicted between timed steps (256 MB write + 256 MB read, outside the per-step events)",
+                    "per_step_counts": {"n_nb": n_nb, "n_c": n_c, "n_w": n_w, "n_wall": n_wall,
+                                        "rebuilds": d["rebuilds"]},
+                    "wall_s": t_wall},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": kname + " (fused contact + capillary + wall + integrate)",
                          "bytes_per_particle": bytes_per_particle, "kernel_ms": ms_k.value},
+            "rebuild": rebuild,
             "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": cpu_sample},
             "contact_evaluations_per_s": value * n_c,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": n * 72, "d2h_bytes_per_step": n * 96},
-            "gpu_launches": launches_per_step * steps + rebuild_launches * d["rebuilds"],
+            "e2e_parts_ms": e2e_parts,
+            "gpu_launches": launches_per_step * args.steps + rebuild_launches * d["rebuilds"],
             "clocks": ck,
             "accuracy_vs_fp64": accuracy,
             "reference_kernels_gpu": ref_gpu,
@@ -924,6 +822,206 @@ def main():
     eng.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def rebuild_cost(eng, n: int) -> dict:
+    """one forced rebuild of engine e timed kernel by kernel, and the rebuild
+    interval seen so far: the rebuild's share of a step, amortised"""
+    prof = eng.profile_kernels()
+    ms = sum(t for name, t in prof if name != "step kernel")
+    st = eng.stats()
+    per = st["iter"] / max(1, st["rebuilds"])
+    return {"rebuild_ms": ms, "steps_per_rebuild_so_far": per, "amortised_ms_per_step": ms / per,
+            "kernels": {name: t for name, t in prof}}
+
+
+def end_to_end(eng, n: int, steps: int, ws: int) -> tuple[float, dict]:
+    """particle-steps/s through dem_set_state_ex + dem_step + dem_get_state with
+    pinned host buffers (state in, one step, state and force out), and where
+    the time of such a step goes (dem_e2e_parts)"""
+    import ctypes as C
+
+    import torch
+
+    from gpucode_gb300._abi import check, ptr
+
+    hp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hv = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hw = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hf = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    check(eng.lib.dem_get_state(eng.h, ptr(hp), ptr(hv), ptr(hw), None, None), "dem_get_state")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        check(eng.lib.dem_set_state_ex(eng.h, ptr(hp), ptr(hv), ptr(hw), 0), "dem_set_state_ex")
+        check(eng.lib.dem_step(eng.h, 1), "dem_step")
+        check(eng.lib.dem_get_state(eng.h, ptr(hp), ptr(hv), ptr(hw), ptr(hf), None), "dem_get_state")
+    e2e_t = time.perf_counter() - t0
+    rate, _ = replica_rate(e2e_t, n, steps, ws)
+    out = (C.c_double * 9)()
+    check(eng.lib.dem_e2e_parts(eng.h, ptr(hp), ptr(hv), ptr(hw), ptr(hf), 10, out), "dem_e2e_parts")
+    names = ["host_total", "dev_upload_copies", "dev_import_shadows", "dev_to_step_end", "dev_step_to_export",
+             "dev_export_gather_copies", "host_in_set_state", "host_in_step", "host_in_get_state"]
+    return rate, {k: out[i] for i, k in enumerate(names)}
+
+
+def accuracy_runs(w, args, torch) -> dict:
+    """packing fraction and coordination number of the mixed engine against
+    FP64 runs of the reference's formulas from the same bed"""
+    from gpucode_gb300.engine import Engine, packing_metrics
+
+    out = {}
+    runs = {}
+    for name, prec in (("mixed", "mixed"), ("fp64", "fp64")):
+        if args.accuracy_steps <= 0:
+            break
+        e = Engine(w.setup, precision=prec, use_graph=True)
+        e.set_state(w.pos0_reduced)
+        t0 = time.perf_counter()
+        short = min(args.oracle_steps, args.accuracy_steps)
+        if short > 0:
+            e.step(short)
+            runs[name + "_short"] = e.get_state()["pos"]
+        e.step(args.accuracy_steps - short)
+        e.sync()
+        runs[name] = (e.get_state()["pos"], time.perf_counter() - t0)
+        e.close()
+    if runs:
+        mm, mr = packing_metrics(w.setup, runs["mixed"][0]), packing_metrics(w.setup, runs["fp64"][0])
+        out["engines"] = {"steps": args.accuracy_steps, "phi_mixed": mm["phi"], "phi_fp64": mr["phi"],
+                          "phi_rel_err": abs(mm["phi"] - mr["phi"]) / mr["phi"], "z_mixed": mm["z"],
+                          "z_fp64": mr["z"], "z_rel_err": abs(mm["z"] - mr["z"]) / max(mr["z"], 1e-300),
+                          "n_probe": mr["n_probe"],
+                          "fp64_particle_steps_per_s": w.setup.n * args.accuracy_steps / runs["fp64"][1],
+                          "max_position_diff": float(np.abs(runs["mixed"][0] - runs["fp64"][0]).max())}
+    if args.oracle_steps > 0:
+        threads = os.cpu_count() or 1
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pyoracle
+
+        if not pyoracle.ORACLE_LIB.exists():
+            pyoracle.build_oracle()
+        sim = pyoracle.OracleSim(w.setup, w.pos0_reduced)
+        t0 = time.perf_counter()
+        sim.step(args.oracle_steps)
+        t_or = time.perf_counter() - t0
+        po = sim.state()["pos"]
+        sim.close()
+        mo = packing_metrics(w.setup, po)
+        o = {"steps": args.oracle_steps, "phi_oracle": mo["phi"], "z_oracle": mo["z"], "cores": threads,
+             "oracle_particle_steps_per_s": w.setup.n * args.oracle_steps / t_or}
+        for name in ("mixed", "fp64"):
+            key = name + "_short"
+            if key in runs:
+                m = packing_metrics(w.setup, runs[key])
+                o[f"phi_{name}"] = m["phi"]
+                o[f"z_{name}"] = m["z"]
+                o[f"phi_rel_err_{name}"] = abs(m["phi"] - mo["phi"]) / mo["phi"]
+                o[f"z_rel_err_{name}"] = abs(m["z"] - mo["z"]) / max(mo["z"], 1e-300)
+                o[f"max_position_diff_{name}"] = float(np.abs(runs[key] - po).max())
+        out["oracle"] = o
+    return out
+
+
+def learned_closure(w, args, timed_steps, torch, flush) -> dict:
+    import ctypes as C
+
+    from gpucode_gb300 import capnet as cn
+    from gpucode_gb300._abi import check
+    from gpucode_gb300.engine import Engine, packing_metrics
+
+    n = w.setup.n
+    n_snap = 11
+    per_snap = -(-args.capnet_samples // n_snap)
+    xs, ys = [], []
+    e = Engine(w.setup, precision="mixed")
+    e.set_state(w.pos0_reduced)
+    gap = max(1, args.sample_steps // (n_snap + 1))
+    e.step(args.sample_steps - n_snap * gap)
+    for _ in range(n_snap):
+        e.step(gap)
+        x, y = cn.collect_samples(e, per_snap)
+        xs.append(x.clone())
+        ys.append(y.clone())
+    e.close()
+    x = torch.cat(xs).contiguous()
+    y = torch.cat(ys).contiguous()
+    xs, ys = [], []
+    net = cn.CapNet(seed=0)
+    rep = net.fit(x, y, epochs=args.capnet_epochs, batch=8192, lr=1e-3, val_frac=0.1, seed=2024)
+    em = Engine(w.setup, precision="mixed", capillary="mlp", graph_steps=1, pairs=args.pairs,
+                block_size=args.block_size)
+    em.set_capnet(net)
+    em.set_state(w.pos0_reduced)
+    em.step(args.warmup)
+    ms_m, _, ck_m, m0, m1 = timed_steps(em, args.steps, all_ranks=False)
+    value_m = n * args.steps / (ms_m / 1000.0)
+    ms_km = C.c_double()
+    check(em.lib.dem_profile_step(em.h, args.profile_reps, C.c_void_p(flush.data_ptr()), flush.numel(),
+                                  C.byref(ms_km)), "dem_profile_step")
+    kname = em.step_kernel_name()
+    evals, falls = m1["cap_mlp"] - m0["cap_mlp"], m1["cap_fallback"] - m0["cap_fallback"]
+    em.close()
+
+    def per_call_ms(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    big = x[: min(len(x), 2_000_000)].contiguous()
+    nb = len(big)
+    rates = {"network_bf16_tensor_cores": nb / per_call_ms(lambda: net.infer(big, True)) * 1e3,
+             "network_fp32": nb / per_call_ms(lambda: net.infer(big, False)) * 1e3,
+             "formula_fp64_as_reference": nb / per_call_ms(lambda: cn.formula(big, True)) * 1e3,
+             "formula_fp32_step_kernel": nb / per_call_ms(lambda: cn.formula(big, False)) * 1e3}
+    net.close()
+    return {"value": value_m, "unit": UNIT, "ms_per_step": ms_m / args.steps, "kernel": kname,
+            "kernel_ms": ms_km.value, "clocks": ck_m, "samples": len(x), "epochs": rep["epochs"],
+            "fit_seconds": rep["seconds"], "val_mse_standardised": rep["val_mse"],
+            "val_force_rel_err_mean": rep["val_force_rel_mean"], "val_force_rel_err_max": rep["val_force_rel_max"],
+            "val_rupture_rel_err_max": rep["val_rupture_rel_max"], "rebuilds": m1["rebuilds"] - m0["rebuilds"],
+            "network_evaluations_per_step": evals / args.steps,
+            "formula_fallback_fraction": falls / max(evals + falls, 1), "evaluations_per_s": rates}
+
+
+def reference_kernels(w, args, flush, value, closure, kernel_ms) -> dict:
+    """the reference's kernel.cu, built for sm_103a, driven in main.cpp's step
+    order from the same bed (after the same warm-up) on this GPU"""
+    from baseline import refgpu
+
+    from gpucode_gb300.engine import Engine
+
+    n = w.setup.n
+    ok, why = refgpu.available()
+    if not ok:
+        return {"unavailable": why}
+    e = Engine(w.setup, precision="mixed")
+    e.set_state(w.pos0_reduced)
+    e.step(args.warmup)
+    stt = e.get_state()
+    e.close()
+    try:
+        r, _ = refgpu.run(w.setup, stt["pos"], stt["vel"], stt["angvel"], 5, args.ref_gpu_steps,
+                          flush.data_ptr(), flush.numel())
+    except RuntimeError as ex:
+        return {"unavailable": str(ex)}
+    rv = n / (r["step_ms"] * 1e-3)
+    return {"value": rv, "unit": UNIT, "ms_per_step": r["step_ms"],
+            "kernel_ms": {"PPForceCalcG": r["force_ms"], "CirPWInterG": r["wall_ms"],
+                          "UpdateSystemG": r["update_ms"]},
+            "rebuilds": r["rebuilds"], "slot_overflow": bool(r["overflow"]), "speedup": value / rv,
+            "speedup_with_learned_closure": closure["value"] / rv if closure else None,
+            "kernel_speedup": (r["force_ms"] + r["wall_ms"] + r["update_ms"]) / kernel_ms,
+            "sample": f"{args.ref_gpu_steps} steps after 5 warm-up from the bed after {args.warmup} steps of this "
+                      "library, histories empty, L2 evicted before each step, main.cpp step order (per-step flag "
+                      "read, VarInit memsets)"}
 
 
 if __name__ == "__main__":

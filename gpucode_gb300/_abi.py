@@ -227,6 +227,8 @@ def _declare(lib: C.CDLL) -> None:
         "dem_get_stats": (I, [P, C.POINTER(DemStats)]),
         "dem_stream": (P, [P]),
         "dem_step_chained": (I, [P]),
+        "dem_step_kernel": (C.c_char_p, [P]),
+        "dem_e2e_parts": (I, [P, P, P, P, P, I, P]),
         "dem_get_neighbors": (I, [P, P, P, I]),
         "dem_get_history": (I, [P, P, P, I]),
         "dem_get_aux": (I, [P, P, P, P, P, P, P]),

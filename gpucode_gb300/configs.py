@@ -52,10 +52,35 @@ class Workload:
     pos0: np.ndarray  # SI initial positions (N, 3)
     setup: Setup
     steps: int
+    pos_reduced: np.ndarray | None = None  # the start in reduced units, when it was stored that way
 
     @property
     def pos0_reduced(self) -> np.ndarray:
+        if self.pos_reduced is not None:
+            return self.pos_reduced
         return self.setup.to_reduced(self.pos0)
+
+
+def load_bed(path, steps: int = 0) -> Workload:
+    """A bed stored by tests/golden/make_packed_bed.py: the dem_setup struct's
+    bytes, the per-particle radius, size level and level rank, and the start
+    positions in reduced units.  Reads the file only: nothing here loads
+    libdem_gb300, so the oracle can be run on the bed without the library."""
+    import json
+
+    f = np.load(path)
+    s = _abi.DemSetup()
+    raw = f["setup"].tobytes()
+    if len(raw) != C.sizeof(s) or int(f["setup_size"]) != C.sizeof(s):
+        raise ValueError(f"{path}: dem_setup of {len(raw)} bytes, this build's is {C.sizeof(s)}")
+    C.memmove(C.addressof(s), raw, len(raw))
+    setup = Setup(s, np.ascontiguousarray(f["rad"], np.float64), np.ascontiguousarray(f["plevel"], np.int32),
+                  np.ascontiguousarray(f["nidx"], np.int32))
+    pos = np.ascontiguousarray(f["pos"], np.float64)
+    rl = s.unit.rlunit
+    recipe = json.loads(str(f["recipe"])) if "recipe" in f else {}
+    return Workload(f"bed{setup.n}", None, 2.0 * setup.rad * rl, pos * rl, setup, steps or recipe.get("steps", 0),
+                    pos_reduced=pos)
 
 
 PI_REF = 3.1415926  # the reference's PI (heydem.h:15), used by its constant derivations

@@ -23,6 +23,7 @@
  * mixed.cu.
  */
 #include <cuda_runtime.h>
+#include <chrono>
 
 #include <algorithm>
 #include <cmath>
@@ -797,6 +798,12 @@ extern "C" void* dem_stream(dem_ctx* c) { return c ? (void*)c->stream : nullptr;
 
 extern "C" int dem_step_chained(dem_ctx* c) { return c && c->chain_state == 1 ? 1 : 0; }
 
+extern "C" const char* dem_step_kernel(dem_ctx* c) {
+  if (!c) return "";
+  if (c->opt.precision == DEM_PREC_MIXED) return mixed_step_kernel_name(c);
+  return "k_pp_force64 + k_wall_force64 + k_update64";
+}
+
 extern "C" dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel) {
   return dem_set_state_ex(c, pos, vel, angvel, 1);
 }
@@ -808,11 +815,13 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
   EngineBufs& b = c->b;
   /* host arrays (caller order) go to the tmp buffers (copy engine), then a
    * gather by id into cell order */
+  if (c->trace) cudaEventRecord(c->trace[0], c->stream);
   cudaError_t e = cudaMemcpyAsync(b.tmp_pos, pos, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && vel) e = cudaMemcpyAsync(b.tmp_vel, vel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && angvel)
     e = cudaMemcpyAsync(b.tmp_angv, angvel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaEventRecord(c->xev[0], c->stream);
+  if (e == cudaSuccess && c->trace) e = cudaEventRecord(c->trace[1], c->stream);
   if (e != cudaSuccess) return cuda_check(e, "dem_set_state upload");
   k_import<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_pos, b.tmp_vel, b.tmp_angv, b.pos, b.vel,
                                                          b.angv, vel != nullptr, angvel != nullptr);
@@ -826,6 +835,7 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
     if (st == DEM_OK) st = mixed_shadows(c, c->parity, c->stream);
     if (st != DEM_OK) return st;
   }
+  if (c->trace) cudaEventRecord(c->trace[2], c->stream);
   /* the caller's arrays are free again once the copies are done; the import
    * and the shadows run on behind them, ahead of the next step */
   e = cudaEventSynchronize(c->xev[0]);
@@ -837,6 +847,7 @@ extern "C" dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, doub
   if (!c) return fail(DEM_ERR_ARG, "dem_get_state: null context");
   EngineBufs& b = c->b;
   const size_t N = (size_t)c->n;
+  if (c->trace) cudaEventRecord(c->trace[4], c->stream);
   if (c->opt.precision == DEM_PREC_MIXED && (force || mom)) {
     dem_status st = mixed_force_to_master(c, c->stream);
     if (st != DEM_OK) return st;
@@ -864,13 +875,25 @@ extern "C" dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, doub
     k++;
   }
   if (e == cudaSuccess) e = cudaEventRecord(c->xev[6], c->xfer);
+  if (e == cudaSuccess && c->trace) e = cudaEventRecord(c->trace[5], c->xfer);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->xev[6], 0);
   if (e != cudaSuccess) return cuda_check(e, "dem_get_state");
   return cuda_check(cudaEventSynchronize(c->xev[6]), "dem_get_state");
 }
 
+namespace {
+dem_status step_calls(dem_ctx* c, int nsteps);
+}
+
 extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return fail(DEM_ERR_ARG, "dem_step: bad argument");
+  dem_status st = step_calls(c, nsteps);
+  if (st == DEM_OK && c->trace) cudaEventRecord(c->trace[3], c->stream);
+  return st;
+}
+
+namespace {
+dem_status step_calls(dem_ctx* c, int nsteps) {
   dem_status st = DEM_OK;
   int left = nsteps;
   if (c->opt.use_graph && c->opt.precision == DEM_PREC_MIXED && c->n > 0 && c->chain_state >= 0 && nsteps > 0) {
@@ -945,6 +968,60 @@ extern "C" dem_status dem_step(dem_ctx* c, int nsteps) {
     if (st != DEM_OK) return st;
     left--;
   }
+  return DEM_OK;
+}
+}  // namespace
+
+extern "C" dem_status dem_e2e_parts(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,
+                                    int reps, double* out) {
+  if (!c || !pos || !vel || !angvel || !force || !out || reps <= 0)
+    return fail(DEM_ERR_ARG, "dem_e2e_parts: bad argument");
+  if (c->trace) return fail(DEM_ERR_STATE, "dem_e2e_parts: already tracing");
+  cudaEvent_t ev[6] = {};
+  cudaError_t e = cudaSuccess;
+  for (cudaEvent_t& x : ev)
+    if (e == cudaSuccess) e = cudaEventCreate(&x);
+  if (e != cudaSuccess) {
+    for (cudaEvent_t x : ev)
+      if (x) cudaEventDestroy(x);
+    return cuda_check(e, "dem_e2e_parts: cudaEventCreate");
+  }
+  double acc[9] = {};
+  dem_status st = dem_sync(c);
+  for (int r = 0; r < reps && st == DEM_OK; r++) {
+    c->trace = ev;
+    const auto t0 = std::chrono::steady_clock::now();
+    st = dem_set_state_ex(c, pos, vel, angvel, 0);
+    const auto t1 = std::chrono::steady_clock::now();
+    if (st == DEM_OK) st = dem_step(c, 1);
+    const auto t2 = std::chrono::steady_clock::now();
+    if (st == DEM_OK) st = dem_get_state(c, pos, vel, angvel, force, nullptr);
+    const auto t3 = std::chrono::steady_clock::now();
+    c->trace = nullptr;
+    if (st != DEM_OK) break;
+    float ms[5] = {};
+    e = cudaEventElapsedTime(&ms[0], ev[0], ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[2], ev[2], ev[3]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[3], ev[3], ev[4]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[4], ev[4], ev[5]);
+    if (e != cudaSuccess) {
+      st = cuda_check(e, "dem_e2e_parts: cudaEventElapsedTime");
+      break;
+    }
+    const auto msd = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+      return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    acc[0] += msd(t0, t3);
+    for (int k = 0; k < 5; k++) acc[1 + k] += ms[k];
+    acc[6] += msd(t0, t1);
+    acc[7] += msd(t1, t2);
+    acc[8] += msd(t2, t3);
+  }
+  c->trace = nullptr;
+  for (cudaEvent_t x : ev) cudaEventDestroy(x);
+  if (st != DEM_OK) return st;
+  for (int k = 0; k < 9; k++) out[k] = acc[k] / reps;
   return DEM_OK;
 }
 

@@ -119,6 +119,10 @@ struct dem_ctx {
   /* dem_profile_kernels: when set, the rebuild and the step record an event
    * after each of their kernels (NULL otherwise, and always during capture) */
   std::vector<std::pair<const char*, cudaEvent_t>>* marks;
+  /* dem_e2e_parts: when set, six timing events the host-facing calls record
+   * at their boundaries (upload start, upload copies done, import queued,
+   * step queued, export start, export copies done); NULL otherwise */
+  cudaEvent_t* trace;
   /* learned capillary closure (DEM_CAP_MLP): the staged network on the device
    * (NULL until dem_set_capnet) and the particles' contact angles */
   void* cap_w;
@@ -137,6 +141,10 @@ dem_status mixed_shadows(dem_ctx* c, int which, cudaStream_t s);
 Prefilter mixed_prefilter(dem_ctx* c, int which);
 /* one fused step reading shadows `which`, writing shadows 1 - which */
 dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s);
+/* the mixed step's pair loop: one thread per particle (true) or warp-cooperative */
+bool mixed_thread_loop(const dem_ctx* c);
+/* the name of the step kernel mixed_step launches, e.g. "k_step_mixed<1,0>" */
+const char* mixed_step_kernel_name(const dem_ctx* c);
 /* copy the last step's bridge counts from the shadow `which` to the master */
 dem_status mixed_pre_rebuild(dem_ctx* c, int which, cudaStream_t s);
 /* download the last step's force totals into the FP64 force array */

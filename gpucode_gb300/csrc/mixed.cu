@@ -1322,6 +1322,18 @@ Prefilter mixed_prefilter(dem_ctx* c, int which) {
   return Prefilter{c->mx->phi[which], 0.5f * c->mx->coarse_tol + 2.0e-6f};
 }
 
+bool mixed_thread_loop(const dem_ctx* c) {
+  const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;
+  return c->opt.pair_mode == DEM_PAIRS_THREAD || (c->opt.pair_mode == DEM_PAIRS_AUTO && net);
+}
+
+const char* mixed_step_kernel_name(const dem_ctx* c) {
+  const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;
+  const bool wet = c->s.force_cap == 1;
+  if (mixed_thread_loop(c)) return net ? "k_step_mixed<1,1>" : wet ? "k_step_mixed<1,0>" : "k_step_mixed<0,0>";
+  return net ? "k_step_coop<1,1>" : wet ? "k_step_coop<1,0>" : "k_step_coop<0,0>";
+}
+
 dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   MixedState* m = c->mx;
   EngineBufs& b = c->b;
@@ -1362,7 +1374,7 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   a.gate = c->step_gate;
   const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;
   if (net && !c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
-  const bool thread_loop = c->opt.pair_mode == DEM_PAIRS_THREAD || (c->opt.pair_mode == DEM_PAIRS_AUTO && net);
+  const bool thread_loop = mixed_thread_loop(c);
   /* threads per block: the option (a multiple of 32 up to 128), else the
    * fastest measured on the 200k wet bed: one warp for the warp-cooperative
    * loop (a block frees its slot as soon as its only warp is done; 75.0 vs

@@ -154,6 +154,10 @@ class Engine:
         """whether the steps launch one another on the device (after the first step)"""
         return bool(self.lib.dem_step_chained(self.h))
 
+    def step_kernel_name(self) -> str:
+        """the step kernel dem_step launches for this engine's options"""
+        return self.lib.dem_step_kernel(self.h).decode()
+
     def neighbors(self, max_per: int = 256) -> tuple[np.ndarray, np.ndarray]:
         counts = np.zeros(self.n, np.int32)
         partners = np.full((self.n, max_per), -1, np.int32)

@@ -344,6 +344,21 @@ void* dem_stream(dem_ctx* c);
  * precision with graphs, after the first dem_step), 0 when they run as
  * host-launched graphs with a conditional rebuild node or host-driven. */
 int dem_step_chained(dem_ctx* c);
+/* Name of the step kernel(s) dem_step launches for this context's precision,
+ * closure and pair loop, e.g. "k_step_mixed<1,0>" (a static string). */
+const char* dem_step_kernel(dem_ctx* c);
+/* Where the time of one end-to-end step goes: `reps` times the host-facing
+ * sequence dem_set_state_ex(pos, vel, angvel, no rebuild request) ->
+ * dem_step(1) -> dem_get_state(pos, vel, angvel, force) on pinned or pageable
+ * host arrays, with timing events at the calls' boundaries.  out[9], each the
+ * mean in ms: [0] host wall time of the sequence; device spans [1] upload
+ * copies, [2] import and shadows (plus the host's return), [3] from the
+ * import to the end of the step (the host's launch of the step included),
+ * [4] from the step to the export's start, [5] export gathers and copies;
+ * host time inside [6] dem_set_state_ex, [7] dem_step, [8] dem_get_state.
+ * The state goes round trip unchanged but for the steps taken. */
+dem_status dem_e2e_parts(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force, int reps,
+                         double* out);
 /* Current neighbour lists in the reference's terms: for every particle i (in
  * the caller's order) its partners (caller's ids) in the reference's list order.
  * counts[np]; partners[np*max_per] (row i = partners of i).  Returns

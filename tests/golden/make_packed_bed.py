@@ -14,10 +14,12 @@ Recipe (needs a GPU; the library steps the bed):
   3. the wet set-up itself (friction 0.3, capillary bridges, dt 5e-7 s) takes the
      bed over from rest for --wet-steps, so its bridges and springs form and the
      bed relaxes under them.
-The file holds the final positions (float64, reduced units, caller order), the
-wet set-up (the dem_setup struct's bytes, the per-particle radius, size level and
-level rank) and the SI diameters.  Velocities and contact histories are not kept:
-a run starts from this bed at rest with empty histories.
+The file holds the final positions (float64, reduced units, caller order) and
+the wet set-up (the dem_setup struct's bytes, the per-particle radius, size level
+and level rank); the diameters are the wet workload's seeded draw
+(configs.lognormal_diameters), which a reader can repeat to check the set-up.
+Velocities and contact histories are not kept: a run starts from this bed at rest
+with empty histories.
 
     python tests/golden/make_packed_bed.py --out tests/golden/packed_wet200k.npz
 """
@@ -92,7 +94,7 @@ def main():
     e.close()
     s = w.setup
     np.savez_compressed(
-        args.out, pos=pos.astype(np.float64), rad=s.rad, plevel=s.plevel, nidx=s.nidx, dia_m=w.dia,
+        args.out, pos=pos.astype(np.float64), rad=s.rad, plevel=s.plevel, nidx=s.nidx,
         setup=np.frombuffer(C.string_at(C.addressof(s.s), C.sizeof(s.s)), np.uint8),
         setup_size=np.int64(C.sizeof(s.s)), log=np.array(json.dumps(log)),
         recipe=np.array(json.dumps({"n": args.n, "cyl_r_m": args.cyl_r, "dry_steps": done, "dry_dt_s": 1e-6,
