@@ -134,6 +134,15 @@ class DemStats(C.Structure):
                 ("cap_fallback", C.c_longlong)]
 
 
+LIQUID_REFERENCE = 0
+LIQUID_PER_CONTACT = 1
+
+
+class DemLiquidModel(C.Structure):
+    _fields_ = [("mode", C.c_int), ("pad", C.c_int), ("vol_min", C.c_double), ("vol_max", C.c_double),
+                ("theta_max", C.c_double), ("seed", C.c_ulonglong)]
+
+
 class DemMemory(C.Structure):
     _fields_ = [("per_particle", C.c_longlong), ("per_slot", C.c_longlong), ("per_cell", C.c_longlong),
                 ("slots", C.c_longlong), ("total", C.c_longlong)]
@@ -173,7 +182,8 @@ _LAYOUT = [
     DemSetup.cyl.offset, DemSetup.mat.offset, DemSetup.prm.offset, DemSetup.unit.offset, DemSetup.sim.offset,
     DemSetup.load.offset, DemSetup.level_size.offset, DemSetup.grid_size.offset, DemSetup.sys_ncells.offset,
     DemSetup.n_pp_slots.offset, DemSetup.rad_max.offset, C.sizeof(DemOptions), C.sizeof(DemStats),
-    C.sizeof(PPCONTACT_HISTORY), C.sizeof(PWCONTACT_HISTORY), C.sizeof(SEARCHCELL),
+    C.sizeof(PPCONTACT_HISTORY), C.sizeof(PWCONTACT_HISTORY), C.sizeof(SEARCHCELL), C.sizeof(DemLiquidModel),
+    DemLiquidModel.seed.offset,
 ]
 
 _lib = None
@@ -229,6 +239,7 @@ def _declare(lib: C.CDLL) -> None:
         "dem_step_chained": (I, [P]),
         "dem_step_kernel": (C.c_char_p, [P]),
         "dem_e2e_parts": (I, [P, P, P, P, P, I, P]),
+        "dem_set_liquid_model": (I, [P, C.POINTER(DemLiquidModel)]),
         "dem_get_neighbors": (I, [P, P, P, I]),
         "dem_get_history": (I, [P, P, P, I]),
         "dem_get_aux": (I, [P, P, P, P, P, P, P]),

@@ -101,14 +101,16 @@ class CapNet:
         return y
 
 
-def formula(x, fp64: bool = True):
+def formula(x, fp64: bool = True, angle: bool = False):
     """the plain closure on raw features (FP64 as the reference evaluates it, or
-    the step kernel's FP32 form), as a float32 CUDA tensor [n][2]"""
+    the step kernel's FP32 form; angle: the per-contact liquid model's
+    regression with the contact angle of feature 2), as a float32 CUDA tensor [n][2]"""
     import torch
 
     y = torch.empty((x.shape[0], 2), dtype=torch.float32, device=x.device)
     lib = _abi.load()
-    check(lib.dem_capnet_formula(_dev(x), int(x.shape[0]), 1 if fp64 else 0, _dev(y)), "dem_capnet_formula")
+    mode = (1 if fp64 else 0) | (2 if angle else 0)
+    check(lib.dem_capnet_formula(_dev(x), int(x.shape[0]), mode, _dev(y)), "dem_capnet_formula")
     return y
 
 

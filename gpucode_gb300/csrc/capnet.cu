@@ -87,6 +87,7 @@ struct SampleArgs {
   double vol, gapmn, layer, stension;
   float theta_max;
   unsigned long long theta_seed;
+  LiquidModel lm; /* mode 1: per-contact volumes and angles (liquid.cuh) */
 };
 
 __global__ void k_sample_count(SampleArgs a, int* cnt) {
@@ -142,19 +143,30 @@ __global__ void k_sample_write(SampleArgs a, const long long* off, long long cap
     const double rj = a.rad[j];
     const double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const double gap = sqrt(dx * dx + dy * dy + dz * dz) - (ri + rj);
-    const int jnl = max(12, a.lqd[j]);
-    const double jVol = a.vol * (8.0 * rj * rj * rj) / jnl;
-    const double ijVol = iVol + jVol;
     const double Splus = gap < 0.0 ? 0.0 : gap;
     const double effR = 2.0 * ri * rj / (ri + rj);
-    const double F = fcap64(Splus, 8.0 * ijVol, effR, lq); /* kernel.cu:538-544 */
     const double thj = cap_theta(a.id[j], a.theta_seed, a.theta_max);
-    x[4 * o + 0] = (float)fmax(a.gapmn, Splus);
-    x[4 * o + 1] = (float)(8.0 * ijVol);
-    x[4 * o + 2] = 0.5f * (thi + (float)thj);
     x[4 * o + 3] = (float)(fmin(ri, rj) / fmax(ri, rj));
-    y[2 * o + 0] = (float)(F / (2.0 * kPiRef * effR * a.stension));
-    y[2 * o + 1] = (float)(0.99 * pow(ijVol, 0.33)); /* kernel.cu:518 */
+    if (a.lm.mode == 0) {
+      const int jnl = max(12, a.lqd[j]);
+      const double jVol = a.vol * (8.0 * rj * rj * rj) / jnl;
+      const double ijVol = iVol + jVol;
+      const double F = fcap64(Splus, 8.0 * ijVol, effR, lq); /* kernel.cu:538-544 */
+      x[4 * o + 0] = (float)fmax(a.gapmn, Splus);
+      x[4 * o + 1] = (float)(8.0 * ijVol);
+      x[4 * o + 2] = 0.5f * (thi + (float)thj);
+      y[2 * o + 0] = (float)(F / (2.0 * kPiRef * effR * a.stension));
+      y[2 * o + 1] = (float)(0.99 * pow(ijVol, 0.33)); /* kernel.cu:518 */
+    } else {
+      /* the per-contact model: the network learns the contact-angle terms too */
+      const double th = 0.5 * ((double)thi + thj);
+      const double V = pair_bridge_volume(a.lm, a.id[q], a.id[j], fmin(ri, rj));
+      x[4 * o + 0] = (float)fmax(a.gapmn, Splus);
+      x[4 * o + 1] = (float)(8.0 * V);
+      x[4 * o + 2] = (float)th;
+      y[2 * o + 0] = (float)willett64(fmax(a.gapmn, Splus), 8.0 * V, th);
+      y[2 * o + 1] = (float)rupture64(V, th);
+    }
     o++;
   }
 }
@@ -361,19 +373,31 @@ __global__ void __launch_bounds__(128) k_infer_tc(const CapNetSmem* __restrict__
 
 /* the plain closure on raw features: FP64 as the reference evaluates it
  * (kernel.cu:65-81 with pow/log/exp, :518), or the step kernel's FP32 form */
-__global__ void k_formula64(const float* __restrict__ xr, long long n, float* __restrict__ y) {
+__global__ void k_formula64(const float* __restrict__ xr, long long n, float* __restrict__ y, int angle) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
+  const double v = xr[4 * q + 1];
+  if (angle) { /* the per-contact model's regression with the contact-angle terms */
+    const double t = xr[4 * q + 2];
+    y[2 * q] = (float)willett64((double)xr[4 * q], v, t);
+    y[2 * q + 1] = (float)rupture64(v / 8.0, t);
+    return;
+  }
   LIQUID unit;
   unit.stension = 1.0; unit.vol = 0.0; unit.gapmn = 0.0; unit.layer = 0.0; unit.brknmx = 0.0;
-  const double v = xr[4 * q + 1];
   y[2 * q] = (float)(fcap64((double)xr[4 * q], v, 1.0, unit) / (2.0 * kPiRef));
   y[2 * q + 1] = (float)(0.99 * pow(v / 8.0, 0.33));
 }
-__global__ void k_formula32(const float* __restrict__ xr, long long n, float* __restrict__ y) {
+__global__ void k_formula32(const float* __restrict__ xr, long long n, float* __restrict__ y, int angle) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= n) return;
   const float v = xr[4 * q + 1];
+  if (angle) {
+    const float t = xr[4 * q + 2];
+    y[2 * q] = willett32(xr[4 * q], v, t);
+    y[2 * q + 1] = rupture32(0.125f * v, t);
+    return;
+  }
   y[2 * q] = cap_formula32(xr[4 * q], v);
   y[2 * q + 1] = 0.99f * exp2f(0.33f * __log2f(0.125f * v));
 }
@@ -607,8 +631,9 @@ dem_status dem_capnet_infer(dem_capnet* net, const float* x_dev, long long n, in
 dem_status dem_capnet_formula(const float* x_dev, long long n, int fp64, float* y_dev) {
   if (!x_dev || !y_dev || n < 0) return fail(DEM_ERR_ARG, "dem_capnet_formula: bad arguments");
   if (n == 0) return DEM_OK;
-  if (fp64) k_formula64<<<blocks_for(n, 256), 256>>>(x_dev, n, y_dev);
-  else k_formula32<<<blocks_for(n, 256), 256>>>(x_dev, n, y_dev);
+  const int angle = (fp64 & 2) != 0;
+  if (fp64 & 1) k_formula64<<<blocks_for(n, 256), 256>>>(x_dev, n, y_dev, angle);
+  else k_formula32<<<blocks_for(n, 256), 256>>>(x_dev, n, y_dev, angle);
   dem_status st = ck(cudaGetLastError(), "dem_capnet_formula launch");
   if (st == DEM_OK) st = ck(cudaDeviceSynchronize(), "dem_capnet_formula");
   return st;
@@ -778,6 +803,7 @@ dem_status dem_capnet_samples(dem_ctx* c, float* x_dev, float* y_dev, long long 
   a.vol = c->s.lqd.vol; a.gapmn = c->s.lqd.gapmn; a.layer = c->s.lqd.layer; a.stension = c->s.lqd.stension;
   a.theta_max = c->theta_max;
   a.theta_seed = c->theta_seed;
+  a.lm = c->lm;
   if (st == DEM_OK) {
     k_sample_count<<<blocks_for(c->n, 256), 256, 0, s>>>(a, cnt);
     k_scan_chunks<<<1, 1024, 0, s>>>(cnt, off, c->n, total);

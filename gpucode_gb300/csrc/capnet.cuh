@@ -34,6 +34,8 @@
 
 #include <cstdint>
 
+#include "liquid.cuh"
+
 namespace dem {
 
 constexpr int kCapIn = 4, kCapH = 64, kCapOut = 2;
@@ -41,15 +43,6 @@ constexpr int kCapW1 = 0, kCapB1 = kCapW1 + kCapH * kCapIn, kCapW2 = kCapB1 + kC
               kCapB2 = kCapW2 + kCapH * kCapH, kCapW3 = kCapB2 + kCapH, kCapB3 = kCapW3 + kCapOut * kCapH,
               kCapParams = kCapB3 + kCapOut;
 static_assert(kCapParams == 4610, "parameter count");
-
-/* contact angles: uniform in [0, theta_max] per particle, from a hash of its id */
-__host__ __device__ inline float cap_theta(int id, unsigned long long seed, float theta_max) {
-  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(id + 1);
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  z ^= z >> 31;
-  return theta_max * (float)((double)(z >> 11) * (1.0 / 9007199254740992.0));
-}
 
 /* Standardisation, training hull and the network's BF16 weights as the step
  * kernel stages them in shared memory (row strides padded so that the eight

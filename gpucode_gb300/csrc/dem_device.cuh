@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "dem_internal.h"
+#include "liquid.cuh"
 
 namespace dem {
 
@@ -204,8 +205,8 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
   dR = 0.5 * (rfrc + rfrc) * fN * iRad;
 }
 
-/* capillary bridge force, kernel.cu:65-81 (Mikami et al. 1998 regression at
- * zero contact angle, the reference's coefficients) */
+/* capillary bridge force, kernel.cu:65-81 (the closed-form fit of Willett et
+ * al. 2000 at zero contact angle, the reference's coefficients) */
 __device__ __forceinline__ double fcap64(double Splus, double ijVol, double effectR, const LIQUID& L) {
   Splus = max(L.gapmn, Splus);
   Splus = Splus / pow(ijVol, 0.5);

@@ -10,6 +10,7 @@
 #include <string>
 
 #include "heydem_gb300.h"
+#include "liquid.cuh"
 
 namespace dem {
 
@@ -157,14 +158,17 @@ dem_status history_rotate(HistSoA old_h, HistSoA cur_h, long long count, cudaStr
 /* VarInit (Allocation.cpp:308-317) as one kernel */
 dem_status var_init(double3* force, double3* mom, double* rmom, int* lqd, int* lqd_old, int n,
                     cudaStream_t stream);
-/* PPForceCalcG (kernel.cu:413-552); H = HistSoA (reference layout) or HistAoS */
+/* PPForceCalcG (kernel.cu:413-552); H = HistSoA (reference layout) or HistAoS.
+ * lm: the liquid model (mode 0: the reference's); id: each particle's caller
+ * id for the per-contact model's hashes (NULL: the index itself) */
 template <class H>
 dem_status pp_force64(const double3* pos, const double3* vel, const double3* angvel,
                       const double* rad, const int* nebor, const int* plevel,
                       const int* level_npars, const int* level_nnebors, const int* nebor_idx,
                       H h, const int* num_nebor, int* lqd, const int* lqd_old,
                       double3* force, double3* mom, double* rmom, int n, int force_cap, int stage,
-                      const DevConsts& k, unsigned long long* counters, cudaStream_t stream);
+                      const DevConsts& k, unsigned long long* counters, cudaStream_t stream,
+                      const int* id = nullptr, LiquidModel lm = LiquidModel{0, 0.f, 0.0, 0.0, 0ull});
 /* CirPWInterG (kernel.cu:958-1023).  move_wall: advance the top wall first
  * (the reference's particle-0 thread does this inside the kernel). */
 template <class H>

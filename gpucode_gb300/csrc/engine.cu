@@ -325,7 +325,7 @@ dem_status enqueue_step(dem_ctx* c, cudaStream_t s, int parity) {
   if (st != DEM_OK) return st;
   st = pp_force64<HistAoS>(b.pos, b.vel, b.angv, b.rad, b.nebor, b.plevel, b.npars, b.nneb, b.nidx, hist_pp(c),
                            b.num_nebor, b.lqd, b.lqd_old, b.force, b.mom, b.rmom, n, c->s.force_cap,
-                           c->s.load_stage, c->k, b.counters, s);
+                           c->s.load_stage, c->k, b.counters, s, b.id, c->lm);
   if (st != DEM_OK) return st;
   st = wall_force64<HistAoS>(b.pos, b.vel, b.angv, b.force, b.mom, b.rmom, b.rad, b.cyl, hist_pw(c), b.nwall,
                              b.wlist, 3 * sizeof(int), n, n, c->s.load_stage, c->k, b.counters,
@@ -802,6 +802,29 @@ extern "C" const char* dem_step_kernel(dem_ctx* c) {
   if (!c) return "";
   if (c->opt.precision == DEM_PREC_MIXED) return mixed_step_kernel_name(c);
   return "k_pp_force64 + k_wall_force64 + k_update64";
+}
+
+extern "C" dem_status dem_set_liquid_model(dem_ctx* c, const dem_liquid_model* m) {
+  if (!c || !m) return fail(DEM_ERR_ARG, "dem_set_liquid_model: null argument");
+  if (m->mode != DEM_LIQUID_REFERENCE && m->mode != DEM_LIQUID_PER_CONTACT)
+    return fail(DEM_ERR_ARG, "dem_set_liquid_model: unknown mode " + std::to_string(m->mode));
+  if (m->mode == DEM_LIQUID_PER_CONTACT &&
+      !(m->vol_min > 0.0 && m->vol_max >= m->vol_min && m->vol_max < 1.0 && m->theta_max >= 0.0 &&
+        m->theta_max < 1.5707963267948966))
+    return fail(DEM_ERR_ARG, "dem_set_liquid_model: need 0 < vol_min <= vol_max < 1 and 0 <= theta_max < pi/2");
+  if (c->chain_state != 0 || c->graph_exec[0] || c->graph_exec[1] || c->graph_one[0] || c->graph_one[1])
+    return fail(DEM_ERR_STATE, "dem_set_liquid_model: set the liquid model before the first dem_step");
+  c->lm.mode = m->mode;
+  c->lm.vol_min = m->vol_min;
+  c->lm.vol_max = m->vol_max;
+  c->lm.theta_max = (float)m->theta_max;
+  c->lm.seed = m->seed;
+  /* the learned closure's contact-angle input is the same per-particle angle */
+  if (m->mode == DEM_LIQUID_PER_CONTACT) {
+    c->theta_max = (float)m->theta_max;
+    c->theta_seed = m->seed;
+  }
+  return DEM_OK;
 }
 
 extern "C" dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel) {

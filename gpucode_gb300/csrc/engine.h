@@ -128,6 +128,8 @@ struct dem_ctx {
   void* cap_w;
   float theta_max;
   unsigned long long theta_seed;
+  /* the liquid-bridge model (dem_set_liquid_model; mode 0: the reference's) */
+  dem::LiquidModel lm;
 };
 
 namespace dem {

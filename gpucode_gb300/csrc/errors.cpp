@@ -74,7 +74,8 @@ extern "C" int dem_abi_layout(long long* out, int cap) {
       (long long)offsetof(dem_setup, n_pp_slots), (long long)offsetof(dem_setup, rad_max),
       (long long)sizeof(dem_options),       (long long)sizeof(dem_stats),
       (long long)sizeof(PPCONTACT_HISTORY), (long long)sizeof(PWCONTACT_HISTORY),
-      (long long)sizeof(SEARCHCELL)};
+      (long long)sizeof(SEARCHCELL),        (long long)sizeof(dem_liquid_model),
+      (long long)offsetof(dem_liquid_model, seed)};
   const int n = (int)(sizeof(v) / sizeof(v[0]));
   for (int i = 0; i < n && i < cap; i++) out[i] = v[i];
   return n;

@@ -102,6 +102,11 @@ struct MixArgs {
   /* a step chained on the device: the rebuild request word; when it is set
    * the step does nothing (it runs again after the rebuild).  NULL otherwise */
   const int* gate;
+  /* the liquid model in FP32 (liquid.cuh): mode 0 the reference's, 1 per-contact
+   * volumes (fraction lq_vmin + lq_vspan u of the smaller sphere) and angles */
+  int lq_mode;
+  float lq_vmin, lq_vspan, lq_theta_max;
+  unsigned long long lq_seed;
 };
 
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
@@ -287,9 +292,17 @@ __device__ __forceinline__ void law32(const Law32& c, float ijRad, float nrm, fl
   r.stage = st;
 }
 
-/* kernel.cu:65-81 in FP32 (the normalised regression: capnet.cuh) */
-__device__ __forceinline__ float fcap32(float Splus, float ijVol, float effR, float gapmn, float st) {
-  return 2.0f * kPiF * effR * st * cap_formula32(fmaxf(gapmn, Splus), ijVol);
+/* a bridge's force magnitude and rupture distance under the context's liquid
+ * model: V the pair's bridge volume (reduced, unscaled), th its contact angle
+ * (per-contact model only).  The reference's model is kernel.cu:65-81 and
+ * :518 in FP32 (the normalised regression: capnet.cuh) */
+__device__ __forceinline__ float bridge_force32(const MixArgs& a, float S, float V, float th, float effR) {
+  const float s = fmaxf(a.lqd_gapmn, S);
+  const float fs = a.lq_mode ? willett32(s, 8.0f * V, th) : cap_formula32(s, 8.0f * V);
+  return 2.0f * kPiF * effR * a.lqd_st * fs;
+}
+__device__ __forceinline__ float bridge_rupture32(const MixArgs& a, float V, float th) {
+  return a.lq_mode ? rupture32(V, th) : 0.99f * exp2f(0.33f * __log2f(V));
 }
 
 __device__ __forceinline__ MixedRec load_rec(const ContactRec* p) {
@@ -625,7 +638,10 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
    * bridges can be queued and evaluated 16 at a time on the tensor cores */
   const int lane = threadIdx.x & 31;
   const int nloop = NET ? __reduce_max_sync(0xffffffffu, nn) : nn;
-  const float th_i = NET ? cap_theta(ro(a.id + qq), a.theta_seed, a.theta_max) : 0.f;
+  const int id_i = (NET || (WET && a.lq_mode)) ? ro(a.id + qq) : 0;
+  const float th_i = (WET && a.lq_mode) ? cap_theta32(id_i, a.lq_seed, a.lq_theta_max)
+                     : NET              ? cap_theta(id_i, a.theta_seed, a.theta_max)
+                                        : 0.f;
   int qn = 0;    /* entries in this warp's queue (warp-uniform) */
   int last = -1; /* this lane's newest entry in it */
   /* one slot ahead: the next partner's index and coarse shadow are in flight
@@ -673,18 +689,28 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
       }
     }
     if (WET && wet_i) {
-      int jnl = __float_as_int(vj4.w);
-      if (jnl < 12) jnl = 12;
-      const float tj = 2.0f * rj;
-      const float jVol = __fdividef(a.lqd_vol * (tj * tj * tj), (float)jnl);
-      float ijVol = iVol + jVol;
+      /* the pair's bridge volume and contact angle: the reference's split of
+       * both particles' liquid, or the per-contact model's */
+      float ijVol, th = 0.f;
+      int id_j = 0;
+      if (a.lq_mode == 0) {
+        int jnl = __float_as_int(vj4.w);
+        if (jnl < 12) jnl = 12;
+        const float tj = 2.0f * rj;
+        ijVol = iVol + __fdividef(a.lqd_vol * (tj * tj * tj), (float)jnl);
+      } else {
+        id_j = ro(a.id + j);
+        th = 0.5f * (th_i + cap_theta32(id_j, a.lq_seed, a.lq_theta_max));
+        ijVol = pair_bridge_volume32(id_i, id_j, a.lq_seed, a.lq_vmin, a.lq_vspan, fminf(ri, rj));
+      }
       const int bprev = a.brg[s];
       const bool form = gap < 2.0f * a.lqd_layer * (ri + rj);
       if (NET && (bprev || form)) {
         /* a bridge to evaluate: queue it for the network, or (outside the
          * network's training box) take the plain formula right here */
         const float sep = fmaxf(a.lqd_gapmn, fmaxf(gap, 0.f)), vol = 8.0f * ijVol;
-        const float theta = 0.5f * (th_i + cap_theta(ro(a.id + j), a.theta_seed, a.theta_max));
+        const float theta =
+            a.lq_mode ? th : 0.5f * (th_i + cap_theta(ro(a.id + j), a.theta_seed, a.theta_max));
         const float ratio = __fdividef(fminf(ri, rj), fmaxf(ri, rj));
         const float effR = 2.0f * ri * rj / (ri + rj);
         if (cap_in_hull(*capw, sep, vol, theta, ratio) && s <= 0xffffffffLL) {
@@ -692,11 +718,10 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
           ent = CapEntry{sep, vol, theta, ratio, wv.x, wv.y, wv.z, gap, (unsigned)s, form ? 1 : 0};
           want = true;
         } else {
-          const float rupture = 0.99f * exp2f(0.33f * __log2f(ijVol));
-          const int b = form ? 1 : (gap > rupture ? 0 : 1);
+          const int b = form ? 1 : (gap > bridge_rupture32(a, ijVol, th) ? 0 : 1);
           a.brg[s] = (unsigned char)b;
           if (b) {
-            const float fc = fcap32(gap < 0.f ? 0.f : gap, vol, effR, a.lqd_gapmn, a.lqd_st);
+            const float fc = bridge_force32(a, gap < 0.f ? 0.f : gap, ijVol, th, effR);
             F.add(u * (-fc));
             wet++;
             if (gap >= 0.f) nbr++;
@@ -704,14 +729,13 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
           nfall++;
         }
       } else if (!NET) {
-        const float rupture = 0.99f * exp2f(0.33f * __log2f(ijVol));
         int b = bprev;
         if (form) b = 1;
-        else if (gap > rupture) b = 0;
+        else if (gap > bridge_rupture32(a, ijVol, th)) b = 0;
         a.brg[s] = (unsigned char)b;
         if (b) {
           const float effR = 2.0f * ri * rj / (ri + rj);
-          const float fc = fcap32(gap < 0.f ? 0.f : gap, ijVol * 8.0f, effR, a.lqd_gapmn, a.lqd_st);
+          const float fc = bridge_force32(a, gap < 0.f ? 0.f : gap, ijVol, th, effR);
           F.add(u * (-fc));
           wet++;
           if (gap >= 0.f) nbr++;
@@ -920,16 +944,24 @@ __device__ __forceinline__ void coop_bridge(const MixArgs& a, const WarpOwn& ow,
                                             bool& want, CapEntry& ent) {
   const float4 hi = ow.hi[o], lo = ow.lo[o];
   const float ri = hi.w + lo.w, rj = g.rj;
-  int jnl = __float_as_int(ro(a.v_in + g.j).w);
-  if (jnl < 12) jnl = 12;
-  const float tj = 2.0f * rj;
-  const float ijVol = ow.v[o].w + __fdividef(a.lqd_vol * (tj * tj * tj), (float)jnl);
+  float ijVol, th = 0.f;
+  if (a.lq_mode == 0) {
+    int jnl = __float_as_int(ro(a.v_in + g.j).w);
+    if (jnl < 12) jnl = 12;
+    const float tj = 2.0f * rj;
+    ijVol = ow.v[o].w + __fdividef(a.lqd_vol * (tj * tj * tj), (float)jnl);
+  } else {
+    const int id_j = ro(a.id + g.j);
+    th = 0.5f * (ow.w[o].w + cap_theta32(id_j, a.lq_seed, a.lq_theta_max));
+    ijVol = pair_bridge_volume32(__float_as_int(ow.v[o].w), id_j, a.lq_seed, a.lq_vmin, a.lq_vspan, fminf(ri, rj));
+  }
   const bool form = (g.meta & kGForm) != 0;
   const float effR = 2.0f * ri * rj / (ri + rj);
   const float vol = 8.0f * ijVol;
   if (NET) {
     const float sep = fmaxf(a.lqd_gapmn, fmaxf(g.gap, 0.f));
-    const float theta = 0.5f * (ow.w[o].w + cap_theta(ro(a.id + g.j), a.theta_seed, a.theta_max));
+    const float theta =
+        a.lq_mode ? th : 0.5f * (ow.w[o].w + cap_theta(ro(a.id + g.j), a.theta_seed, a.theta_max));
     const float ratio = __fdividef(fminf(ri, rj), fmaxf(ri, rj));
     if (cap_in_hull(*capw, sep, vol, theta, ratio) && s <= 0xffffffffLL) {
       const float sc = -2.0f * kPiF * effR * a.lqd_st;
@@ -940,11 +972,10 @@ __device__ __forceinline__ void coop_bridge(const MixArgs& a, const WarpOwn& ow,
     }
     out.flags |= kPFall;
   }
-  const float rupture = 0.99f * exp2f(0.33f * __log2f(ijVol));
-  const int b = form ? 1 : (g.gap > rupture ? 0 : 1);
+  const int b = form ? 1 : (g.gap > bridge_rupture32(a, ijVol, th) ? 0 : 1);
   a.brg[s] = (unsigned char)b;
   if (b) {
-    const float fc = fcap32(g.gap < 0.f ? 0.f : g.gap, vol, effR, a.lqd_gapmn, a.lqd_st);
+    const float fc = bridge_force32(a, g.gap < 0.f ? 0.f : g.gap, ijVol, th, effR);
     out.fx -= g.ux * fc;
     out.fy -= g.uy * fc;
     out.fz -= g.uz * fc;
@@ -1034,8 +1065,15 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_COOP_BLOCKS) k_ste
     const int L = ro(a.plevel + qq);
     ow.hi[lane] = hi;
     ow.lo[lane] = lo;
-    ow.v[lane] = make_float4(vi4.x, vi4.y, vi4.z, iVol);
-    ow.w[lane] = make_float4(wi4.x, wi4.y, wi4.z, NET ? cap_theta(ro(a.id + qq), a.theta_seed, a.theta_max) : 0.f);
+    /* .w of the own velocity: the liquid volume (reference model) or the
+     * particle's id (per-contact model); of the own spin: the contact angle */
+    const bool lqm = WET && a.lq_mode;
+    const int id_i = (NET || lqm) ? ro(a.id + qq) : 0;
+    ow.v[lane] = make_float4(vi4.x, vi4.y, vi4.z, lqm ? __int_as_float(id_i) : iVol);
+    ow.w[lane] = make_float4(wi4.x, wi4.y, wi4.z,
+                             lqm   ? cap_theta32(id_i, a.lq_seed, a.lq_theta_max)
+                             : NET ? cap_theta(id_i, a.theta_seed, a.theta_max)
+                                   : 0.f);
     ow.base[lane] = slot_base(L, a.npars, a.nneb) + ro(a.nidx + qq);
     ow.stride[lane] = ro(a.npars + L);
     LaneAcc z;
@@ -1372,6 +1410,11 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   a.theta_seed = c->theta_seed;
   a.theta_max = c->theta_max;
   a.gate = c->step_gate;
+  a.lq_mode = c->lm.mode;
+  a.lq_vmin = (float)c->lm.vol_min;
+  a.lq_vspan = (float)(c->lm.vol_max - c->lm.vol_min);
+  a.lq_theta_max = c->lm.theta_max;
+  a.lq_seed = c->lm.seed;
   const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;
   if (net && !c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
   const bool thread_loop = mixed_thread_loop(c);

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(128) k_pp_force64(
     const int* __restrict__ nebor_idx, HA h, const int* __restrict__ num_nebor, int* __restrict__ lqd,
     const int* __restrict__ lqd_old, double3* __restrict__ force, double3* __restrict__ mom,
     double* __restrict__ rmom, int n, int force_cap, int stage, DevConsts k,
-    unsigned long long* __restrict__ counters) {
+    unsigned long long* __restrict__ counters, const int* __restrict__ id, LiquidModel lm) {
   /* blocks in reverse: in cell order the largest spheres, with the most
    * pairs, come last (in the reference's order this is only another schedule) */
   const int i = reversed_block_thread();
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(128) k_pp_force64(
       R = R + dR;
       ncontact++;
     }
-    if (force_cap == 1) {
+    if (force_cap == 1 && lm.mode == 0) {
       int jnl = lqd_old[j];
       if (jnl < 12) jnl = 12;
       const double jVol = k.lqd.vol * pow((jr * 2), 3.0) / jnl;
@@ -114,6 +114,24 @@ __global__ void __launch_bounds__(128) k_pp_force64(
         ijVol = ijVol * 8.0;
         const double3 fc = smul3(-1.0 * fcap64(Splus, ijVol, effR, k.lqd), u);
         F = add3(F, fc);
+        wet = wet + 1;
+        if (gap >= 0.0) nbridge++;
+      }
+    } else if (force_cap == 1) {
+      /* per-contact volume and contact angle (liquid.cuh) */
+      const int idi = id ? id[i] : i, idj = id ? id[j] : j;
+      const double th = 0.5 * ((double)cap_theta(idi, lm.seed, lm.theta_max) +
+                               (double)cap_theta(idj, lm.seed, lm.theta_max));
+      const double V = pair_bridge_volume(lm, idi, idj, ir < jr ? ir : jr);
+      int brg = h.brg(ine);
+      if (gap < 2 * k.lqd.layer * (ir + jr)) brg = 1;
+      else if (gap > rupture64(V, th)) brg = 0;
+      h.set_brg(ine, brg);
+      if (brg == 1) {
+        const double Splus = gap < 0 ? 0.0 : gap;
+        const double effR = 2 * ir * jr / (ir + jr);
+        const double fcap = 2 * kPiRef * effR * k.lqd.stension * willett64(max(k.lqd.gapmn, Splus), 8.0 * V, th);
+        F = add3(F, smul3(-1.0 * fcap, u));
         wet = wet + 1;
         if (gap >= 0.0) nbridge++;
       }
@@ -252,13 +270,14 @@ dem_status pp_force64(const double3* pos, const double3* vel, const double3* ang
                       const int* nebor, const int* plevel, const int* level_npars, const int* level_nnebors,
                       const int* nebor_idx, H h, const int* num_nebor, int* lqd, const int* lqd_old,
                       double3* force, double3* mom, double* rmom, int n, int force_cap, int stage,
-                      const DevConsts& k, unsigned long long* counters, cudaStream_t stream) {
+                      const DevConsts& k, unsigned long long* counters, cudaStream_t stream, const int* id,
+                      LiquidModel lm) {
   if (n <= 0) return DEM_OK;
   using HA = typename Acc<H>::T;
   k_pp_force64<HA><<<grid_for(n, 128), 128, 0, stream>>>(pos, vel, angvel, rad, nebor, plevel, level_npars,
                                                         level_nnebors, nebor_idx, Acc<H>::make(h), num_nebor, lqd,
                                                         lqd_old, force, mom, rmom, n, force_cap, stage, k,
-                                                        counters);
+                                                        counters, id, lm);
   return cuda_check(cudaGetLastError(), "pp_force64 launch");
 }
 
@@ -280,11 +299,11 @@ dem_status wall_force64(const double3* pos, const double3* vel, const double3* a
 template dem_status pp_force64<HistSoA>(const double3*, const double3*, const double3*, const double*, const int*,
                                         const int*, const int*, const int*, const int*, HistSoA, const int*, int*,
                                         const int*, double3*, double3*, double*, int, int, int, const DevConsts&,
-                                        unsigned long long*, cudaStream_t);
+                                        unsigned long long*, cudaStream_t, const int*, LiquidModel);
 template dem_status pp_force64<HistAoS>(const double3*, const double3*, const double3*, const double*, const int*,
                                         const int*, const int*, const int*, const int*, HistAoS, const int*, int*,
                                         const int*, double3*, double3*, double*, int, int, int, const DevConsts&,
-                                        unsigned long long*, cudaStream_t);
+                                        unsigned long long*, cudaStream_t, const int*, LiquidModel);
 template dem_status wall_force64<HistSoA>(const double3*, const double3*, const double3*, double3*, double3*,
                                           double*, const double*, CylinderBC*, HistSoA, const int*, const int*,
                                           size_t, int, int, int, const DevConsts&, unsigned long long*, bool,

@@ -175,6 +175,17 @@ class Engine:
         """install a trained CapNet (the engine must use capillary="mlp")"""
         check(self.lib.dem_set_capnet(self.h, net.h), "dem_set_capnet")
 
+    def set_liquid_model(self, mode: str = "per_contact", vol_min: float = 0.005, vol_max: float = 0.02,
+                         theta_max: float = 0.5235987755982988, seed: int = 0) -> None:
+        """dem_set_liquid_model: "reference" (the reference's per-particle liquid,
+        zero contact angle) or "per_contact" (bridge volume a fraction in
+        [vol_min, vol_max] of the smaller sphere, contact angle in [0, theta_max]
+        radians per particle); before the first step"""
+        m = _abi.DemLiquidModel()
+        m.mode = {"reference": _abi.LIQUID_REFERENCE, "per_contact": _abi.LIQUID_PER_CONTACT}[mode]
+        m.vol_min, m.vol_max, m.theta_max, m.seed = float(vol_min), float(vol_max), float(theta_max), int(seed)
+        check(self.lib.dem_set_liquid_model(self.h, C.byref(m)), "dem_set_liquid_model")
+
     def set_contact_angles(self, theta_max_rad: float, seed: int = 0) -> None:
         check(self.lib.dem_set_contact_angles(self.h, float(theta_max_rad), int(seed)), "dem_set_contact_angles")
 

@@ -344,6 +344,29 @@ void* dem_stream(dem_ctx* c);
  * precision with graphs, after the first dem_step), 0 when they run as
  * host-launched graphs with a conditional rebuild node or host-driven. */
 int dem_step_chained(dem_ctx* c);
+/* ---- liquid-bridge model (no counterpart in the reference) ----
+ * DEM_LIQUID_REFERENCE: the reference's (kernel.cu:429-434, :511-544): each
+ * particle's liquid LIQUID.vol (2r)^3 split over max(12, its bridges), the
+ * capillary regression at zero contact angle.
+ * DEM_LIQUID_PER_CONTACT: each unordered pair's bridge volume is a fraction of
+ * the smaller sphere's volume, uniform in [vol_min, vol_max] from a hash of the
+ * two particle ids and the seed; each particle's contact angle is uniform in
+ * [0, theta_max] (radians) from a hash of its id and the seed, a pair takes
+ * the mean; the force is the same regression with its contact-angle terms
+ * (Willett et al. 2000), rupture at (1 + theta/2) 0.99 V^0.33.  Formation,
+ * bridge flags and LIQUID.stension / gapmn / layer are the reference's. */
+#define DEM_LIQUID_REFERENCE 0
+#define DEM_LIQUID_PER_CONTACT 1
+typedef struct dem_liquid_model {
+  int mode;
+  int pad;
+  double vol_min, vol_max;
+  double theta_max;
+  unsigned long long seed;
+} dem_liquid_model;
+/* Set the liquid model (before the first dem_step; both precisions).  It also
+ * sets the learned closure's per-particle contact angles to the model's. */
+dem_status dem_set_liquid_model(dem_ctx* c, const dem_liquid_model* m);
 /* Name of the step kernel(s) dem_step launches for this context's precision,
  * closure and pair loop, e.g. "k_step_mixed<1,0>" (a static string). */
 const char* dem_step_kernel(dem_ctx* c);
@@ -549,8 +572,10 @@ dem_status dem_capnet_grad(dem_capnet* net, const float* x_dev, const float* y_d
  * kernel uses, 0 the FP32 network. */
 dem_status dem_capnet_infer(dem_capnet* net, const float* x_dev, long long n, int tensor_cores, float* y_dev);
 /* The plain closure the network stands in for, on the same raw features:
- * fp64 = 1 as the reference evaluates it (FP64 pow/log/exp), 0 the step
- * kernel's FP32 form. */
+ * bit 0 of fp64 set: FP64 as the reference evaluates it (FP64 pow/log/exp),
+ * clear: the step kernel's FP32 form; bit 1 set: the per-contact liquid
+ * model's regression with the contact angle of feature 2 (the reference's is
+ * the zero-angle case). */
 dem_status dem_capnet_formula(const float* x_dev, long long n, int fp64, float* y_dev);
 /* Install a trained network in a context created with DEM_PREC_MIXED and
  * DEM_CAP_MLP; bridges outside its training box keep the plain formula. */

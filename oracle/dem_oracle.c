@@ -268,9 +268,9 @@ void orc_var_init(ov3* force, ov3* mom, double* rmom, int* lqdCnt, int* lqdCnt_O
 
 /* ===================== contact laws ===================== */
 
-/* kernel.cu:65-81: capillary bridge force; the regression in ln V and ln S+
- * of Mikami et al. (1998) at zero contact angle, with the reference's
- * coefficients. */
+/* kernel.cu:65-81: capillary bridge force; the closed-form regression in
+ * ln V and ln S+ of Willett, Adams, Johnson and Seville (2000, Langmuir
+ * 16:9396) at zero contact angle, with the reference's coefficients. */
 double orc_fcap(double Splus, double ijVol, double effectR, const o_consts* k) {
   Splus = k->lqd.gapmn > Splus ? k->lqd.gapmn : Splus; /* max(gapmn, S+) */
   Splus = Splus / pow(ijVol, 0.5);
@@ -282,6 +282,54 @@ double orc_fcap(double Splus, double ijVol, double effectR, const o_consts* k) {
   return 2 * ORC_PI * effectR * k->lqd.stension *
          exp(f1 - f2 * exp(f3 * log(Splus) + f4 * pow(log(Splus), 2.0)));
 }
+
+/* ---- the per-contact liquid model (no counterpart in the reference) ----
+ * Restates the library's definition: contact angle per particle uniform in
+ * [0, theta_max] from a splitmix64 hash of its id and the seed; a pair's
+ * bridge volume a fraction uniform in [vol_min, vol_max] (a hash of the two
+ * ids, order-free) of the smaller sphere's volume pi/6 (2 r_min)^3 with the
+ * reference's pi; the force the same Willett et al. (2000) fit with its
+ * contact-angle terms (theta in radians); rupture at (1 + theta/2) 0.99 V^0.33
+ * (Lian, Thornton and Adams 1993, on the reference's kernel.cu:518). */
+static unsigned long long orc_mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+float orc_theta(int id, unsigned long long seed, float theta_max) {
+  const unsigned long long z = orc_mix64(seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(id + 1));
+  return theta_max * (float)((double)(z >> 11) * (1.0 / 9007199254740992.0));
+}
+
+double orc_pair_volume(const o_consts* k, int ida, int idb, double r_min) {
+  const unsigned long long lo = (unsigned long long)(ida < idb ? ida : idb);
+  const unsigned long long hi = (unsigned long long)(ida < idb ? idb : ida);
+  const unsigned long long z =
+      orc_mix64(orc_mix64(k->lqd_seed ^ (0xD1B54A32D192ED03ull * (lo + 1))) + 0x9E3779B97F4A7C15ull * (hi + 1));
+  const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  const double f = k->lqd_vol_min + (k->lqd_vol_max - k->lqd_vol_min) * u;
+  const double d = 2.0 * r_min;
+  return f * (3.1415926 / 6.0) * (d * d * d);
+}
+
+double orc_willett(double s, double v, double t) {
+  const double t2 = t * t;
+  const double L = log(v), L2 = L * L, L3 = L2 * L;
+  const double f1 = (-0.44507 + 0.050832 * t - 1.1466 * t2) + (-0.1119 - 0.000411 * t - 0.1490 * t2) * L +
+                    (-0.012101 - 0.0036456 * t - 0.01255 * t2) * L2 +
+                    (-0.0005 - 0.0003505 * t - 0.00029076 * t2) * L3;
+  const double f2 = (1.9222 - 0.57473 * t - 1.2918 * t2) + (-0.0668 - 0.1201 * t - 0.22574 * t2) * L +
+                    (-0.0013375 - 0.0068988 * t - 0.01137 * t2) * L2;
+  const double f3 = (1.268 - 0.01396 * t - 0.23566 * t2) + (0.198 + 0.092 * t - 0.06418 * t2) * L +
+                    (0.02232 + 0.02238 * t - 0.009853 * t2) * L2 + (0.0008585 + 0.001318 * t - 0.00053 * t2) * L3;
+  const double f4 = (-0.010703 + 0.073776 * t - 0.34742 * t2) + (0.03345 + 0.04543 * t - 0.09056 * t2) * L +
+                    (0.0018574 + 0.004456 * t - 0.006257 * t2) * L2;
+  const double ls = log(s / sqrt(v));
+  return exp(f1 - f2 * exp(f3 * ls + f4 * ls * ls));
+}
+
+double orc_rupture(double V, double t) { return (1.0 + 0.5 * t) * (0.99 * pow(V, 0.33)); }
 
 /* Shared normal/tangential law of ContactForceD (kernel.cu:89-228) and
  * PWcontactD (kernel.cu:236-359).  The two differ only in: the effective radius,
@@ -417,7 +465,22 @@ void orc_pp_force(const ov3* pos, const ov3* vel, const ov3* angvel, const doubl
         mom[i] = vadd(mom[i], dM);
         rmom[i] = rmom[i] + dR;
       }
-      if (ForceCap == 1) {
+      if (ForceCap == 1 && k->lqd_mode == 1) {
+        /* the per-contact liquid model (particle index = caller id here) */
+        double th = 0.5 * ((double)orc_theta(i, k->lqd_seed, k->lqd_theta_max) +
+                           (double)orc_theta(j, k->lqd_seed, k->lqd_theta_max));
+        double V = orc_pair_volume(k, i, j, ir < jr ? ir : jr);
+        if (gap < 2 * k->lqd.layer * (ir + jr)) h.lqdBrg[ine] = 1;
+        else if (gap > orc_rupture(V, th)) h.lqdBrg[ine] = 0;
+        if (h.lqdBrg[ine] == 1) {
+          double Splus = (gap < 0) ? 0.0 : gap;
+          double effR = 2 * ir * jr / (ir + jr);
+          double fcap = 2 * ORC_PI * effR * k->lqd.stension *
+                        orc_willett(k->lqd.gapmn > Splus ? k->lqd.gapmn : Splus, 8.0 * V, th);
+          force[i] = vadd(force[i], smul(-1.0 * fcap, u));
+          lqdCnt[i] = lqdCnt[i] + 1;
+        }
+      } else if (ForceCap == 1) {
         int jnl = lqdCnt_Old[j];
         if (jnl < 12) jnl = 12;
         double jVol = k->lqd.vol * pow((jr * 2), 3.0) / jnl;

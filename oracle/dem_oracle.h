@@ -53,13 +53,19 @@ typedef struct { ov3 Origin; ov3 EndPoint; double SearchGap; double dt; int NP; 
 /* heydem.h:220-229 calParaPP (calParaPW has the same layout, heydem.h:233-242) */
 typedef struct { double emod, pois, sfrc, ystress, ydsp_t, yforce_t, ystiff_t; } o_calpara;
 
-/* the constant-memory set of kernel.cu:15-19 */
+/* the constant-memory set of kernel.cu:15-19, then this library's per-contact
+ * liquid model (no counterpart in the reference: lqd_mode 0 is the reference's
+ * model and the reference's own kernels never read these fields) */
 typedef struct {
   o_mat mat[2];
   o_liquid lqd;
   o_parameter prm;
   o_calpara cal;   /* p-p */
   o_calpara pwcal; /* p-wall */
+  int lqd_mode;    /* 0: the reference's; 1: per-contact volumes and contact angles */
+  float lqd_theta_max;
+  double lqd_vol_min, lqd_vol_max;
+  unsigned long long lqd_seed;
 } o_consts;
 
 /* heydem.h:209-214 SEARCHCELL (pointers to per-level arrays) */
@@ -126,6 +132,13 @@ int orc_update(const double* rad, ov3* pos, ov3* vel, ov3* angvel, const ov3* fo
 
 /* single-function probes for the contact laws (known-answer tests) */
 double orc_fcap(double Splus, double ijVol, double effectR, const o_consts* k);
+/* the per-contact liquid model (see dem_oracle.c): a particle's contact angle,
+ * a pair's bridge volume, the regression with its contact-angle terms
+ * (normalised, s = max(gapmn, S), v = 8 V) and the rupture distance */
+float orc_theta(int id, unsigned long long seed, float theta_max);
+double orc_pair_volume(const o_consts* k, int ida, int idb, double r_min);
+double orc_willett(double s, double v, double theta);
+double orc_rupture(double V, double theta);
 
 /* ---- a whole simulation in the reference's layouts: main.cpp:433-568 ---- */
 typedef struct orc_sim orc_sim;

@@ -32,7 +32,9 @@ REF_SRC = reference_dir()
 
 
 class OConsts(C.Structure):
-    _fields_ = [("mat", MatType * 2), ("lqd", LIQUID), ("prm", PARAMETER), ("cal", calPara), ("pwcal", calPara)]
+    _fields_ = [("mat", MatType * 2), ("lqd", LIQUID), ("prm", PARAMETER), ("cal", calPara), ("pwcal", calPara),
+                ("lqd_mode", C.c_int), ("lqd_theta_max", C.c_float), ("lqd_vol_min", C.c_double),
+                ("lqd_vol_max", C.c_double), ("lqd_seed", C.c_ulonglong)]
 
 
 def _declare(lib: C.CDLL) -> C.CDLL:
@@ -52,6 +54,15 @@ def _declare(lib: C.CDLL) -> C.CDLL:
     lib.orc_sim_set_kernels.argtypes = [P, P]
     lib.orc_fcap.restype = C.c_double
     lib.orc_fcap.argtypes = [C.c_double, C.c_double, C.c_double, P]
+    if hasattr(lib, "orc_willett"):
+        lib.orc_willett.restype = C.c_double
+        lib.orc_willett.argtypes = [C.c_double, C.c_double, C.c_double]
+        lib.orc_rupture.restype = C.c_double
+        lib.orc_rupture.argtypes = [C.c_double, C.c_double]
+        lib.orc_theta.restype = C.c_float
+        lib.orc_theta.argtypes = [I, C.c_ulonglong, C.c_float]
+        lib.orc_pair_volume.restype = C.c_double
+        lib.orc_pair_volume.argtypes = [P, I, I, C.c_double]
     return lib
 
 
@@ -136,6 +147,16 @@ class OracleSim:
         self.arr("Nebor_Idx", np.int32, self.n)[:] = setup.nidx
         self.set_state(pos, vel, angvel)
         self.lib.orc_sim_set_mode(self.h, int(s.force_cap), int(s.load_stage))
+
+    def set_liquid_model(self, mode: int, vol_min: float = 0.0, vol_max: float = 0.0, theta_max: float = 0.0,
+                         seed: int = 0) -> None:
+        """the per-contact liquid model (mode 1) or the reference's (mode 0); the
+        same parameters as the library's dem_set_liquid_model"""
+        k = OConsts.from_address(self.lib.orc_sim_ptr(self.h, b"consts"))
+        k.lqd_mode = int(mode)
+        k.lqd_vol_min, k.lqd_vol_max = float(vol_min), float(vol_max)
+        k.lqd_theta_max = float(theta_max)
+        k.lqd_seed = int(seed)
 
     def arr(self, name: str, dtype, count: int) -> np.ndarray:
         p = self.lib.orc_sim_ptr(self.h, name.encode())

@@ -194,8 +194,13 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
     return {"force_err": ferr, "hist_err": herr, "stage_mismatch": st_mis, "tie_particles": ties}
 
 
-def run(eng, w, pos, vel, ang, steps: int, tol: dict, mismatch_budget: float = 0.0) -> dict:
+def run(eng, w, pos, vel, ang, steps: int, tol: dict, mismatch_budget: float = 0.0, liquid: dict | None = None) -> dict:
+    """`steps` steps of engine eng in lockstep with the oracle; liquid: the
+    oracle's per-contact liquid model (OracleSim.set_liquid_model arguments),
+    to match an engine that was given the same one"""
     sim = _harness.OracleSim(w.setup, pos, vel, ang)
+    if liquid:
+        sim.set_liquid_model(**liquid)
     mp = max_per(w)
     eng.set_state(pos, vel, ang)
     worst = {"force_err": 0.0, "hist_err": 0.0, "stage_mismatch": 0.0, "tie_particles": 0}
