@@ -774,6 +774,9 @@ def run_headline(args, ws, rank):
     # the bed, trained by the library's own kernels, then the same bed stepped
     # with the network fused in the step kernel (BF16 tensor-core tiles)
     closure = None
+    liquid = None
+    if rank == 0 and not args.host_steps:
+        liquid = per_contact_liquid(w, args, timed_steps, flush)
     if rank == 0 and args.capnet_samples > 0 and not args.host_steps:
         closure = learned_closure(w, args, timed_steps, torch, flush)
 
@@ -816,6 +819,7 @@ def run_headline(args, ws, rank):
             "clocks": ck,
             "accuracy_vs_fp64": accuracy,
             "reference_kernels_gpu": ref_gpu,
+            "per_contact_liquid": liquid,
             "learned_closure": closure,
         }
         print(json.dumps(line), flush=True)
@@ -924,7 +928,57 @@ def accuracy_runs(w, args, torch) -> dict:
     return out
 
 
+# the configured liquid: bridge volume per contact uniform in [0.5 %, 2 %] of the
+# smaller sphere's volume, contact angle per particle uniform in [0, 30 deg]
+LIQUID_CFG = {"vol_min": 0.005, "vol_max": 0.02, "theta_max": 0.5235987755982988, "seed": 2}
+
+
+def per_contact_liquid(w, args, timed_steps, flush) -> dict:
+    """The bed with the configured per-contact liquid model (FP32 formula with
+    the contact-angle terms): step rate and kernel time, and packing fraction /
+    coordination number against the FP64 engine with the same model"""
+    import ctypes as C
+
+    from gpucode_gb300._abi import check
+    from gpucode_gb300.engine import Engine, packing_metrics
+
+    n = w.setup.n
+    e = Engine(w.setup, precision="mixed", graph_steps=1, pairs=args.pairs, block_size=args.block_size)
+    e.set_liquid_model("per_contact", **LIQUID_CFG)
+    e.set_state(w.pos0_reduced)
+    e.step(args.warmup)
+    ms, _, ck, s0, s1 = timed_steps(e, args.steps, all_ranks=False)
+    ms_k = C.c_double()
+    check(e.lib.dem_profile_step(e.h, args.profile_reps, C.c_void_p(flush.data_ptr()), flush.numel(),
+                                 C.byref(ms_k)), "dem_profile_step")
+    ps = n * args.steps
+    out = {"model": LIQUID_CFG, "value": n * args.steps / (ms / 1000.0), "unit": UNIT,
+           "ms_per_step": ms / args.steps, "kernel": e.step_kernel_name(), "kernel_ms": ms_k.value, "clocks": ck,
+           "bridges_per_particle_step": (s1["bridges"] - s0["bridges"]) / ps,
+           "contacts_per_particle_step": (s1["contacts"] - s0["contacts"]) / ps}
+    e.close()
+    if args.accuracy_steps > 0:
+        pos = {}
+        for prec in ("mixed", "fp64"):
+            e = Engine(w.setup, precision=prec)
+            e.set_liquid_model("per_contact", **LIQUID_CFG)
+            e.set_state(w.pos0_reduced)
+            e.step(args.accuracy_steps)
+            pos[prec] = e.get_state()["pos"]
+            e.close()
+        mm, mr = packing_metrics(w.setup, pos["mixed"]), packing_metrics(w.setup, pos["fp64"])
+        out["accuracy_vs_fp64"] = {"steps": args.accuracy_steps, "phi_mixed": mm["phi"], "phi_fp64": mr["phi"],
+                                   "phi_rel_err": abs(mm["phi"] - mr["phi"]) / mr["phi"], "z_mixed": mm["z"],
+                                   "z_fp64": mr["z"], "z_rel_err": abs(mm["z"] - mr["z"]) / max(mr["z"], 1e-300),
+                                   "max_position_diff": float(np.abs(pos["mixed"] - pos["fp64"]).max())}
+    return out
+
+
 def learned_closure(w, args, timed_steps, torch, flush) -> dict:
+    """The learned capillary closure under the configured per-contact liquid
+    model: samples of the plain formula (with its contact-angle terms) logged
+    from the bed, trained by the library's own kernels, then the bed stepped
+    with the network fused in the step kernel"""
     import ctypes as C
 
     from gpucode_gb300 import capnet as cn
@@ -936,6 +990,7 @@ def learned_closure(w, args, timed_steps, torch, flush) -> dict:
     per_snap = -(-args.capnet_samples // n_snap)
     xs, ys = [], []
     e = Engine(w.setup, precision="mixed")
+    e.set_liquid_model("per_contact", **LIQUID_CFG)
     e.set_state(w.pos0_reduced)
     gap = max(1, args.sample_steps // (n_snap + 1))
     e.step(args.sample_steps - n_snap * gap)
@@ -953,6 +1008,7 @@ def learned_closure(w, args, timed_steps, torch, flush) -> dict:
     em = Engine(w.setup, precision="mixed", capillary="mlp", graph_steps=1, pairs=args.pairs,
                 block_size=args.block_size)
     em.set_capnet(net)
+    em.set_liquid_model("per_contact", **LIQUID_CFG)
     em.set_state(w.pos0_reduced)
     em.step(args.warmup)
     ms_m, _, ck_m, m0, m1 = timed_steps(em, args.steps, all_ranks=False)
@@ -979,8 +1035,16 @@ def learned_closure(w, args, timed_steps, torch, flush) -> dict:
     nb = len(big)
     rates = {"network_bf16_tensor_cores": nb / per_call_ms(lambda: net.infer(big, True)) * 1e3,
              "network_fp32": nb / per_call_ms(lambda: net.infer(big, False)) * 1e3,
-             "formula_fp64_as_reference": nb / per_call_ms(lambda: cn.formula(big, True)) * 1e3,
-             "formula_fp32_step_kernel": nb / per_call_ms(lambda: cn.formula(big, False)) * 1e3}
+             "formula_fp64": nb / per_call_ms(lambda: cn.formula(big, True, angle=True)) * 1e3,
+             "formula_fp32_step_kernel": nb / per_call_ms(lambda: cn.formula(big, False, angle=True)) * 1e3}
+    yn = net.infer(big, True).double()
+    yf = cn.formula(big, True, angle=True).double()
+    y32 = cn.formula(big, False, angle=True).double()
+    rel = lambda a, b: ((a[:, 0] - b[:, 0]).abs() / b[:, 0].abs().clamp_min(1e-30))  # noqa: E731
+    errors = {"network_force_rel_err_mean": float(rel(yn, yf).mean()),
+              "network_force_rel_err_max": float(rel(yn, yf).max()),
+              "fp32_formula_force_rel_err_mean": float(rel(y32, yf).mean()),
+              "fp32_formula_force_rel_err_max": float(rel(y32, yf).max())}
     net.close()
     return {"value": value_m, "unit": UNIT, "ms_per_step": ms_m / args.steps, "kernel": kname,
             "kernel_ms": ms_km.value, "clocks": ck_m, "samples": len(x), "epochs": rep["epochs"],
@@ -988,7 +1052,8 @@ def learned_closure(w, args, timed_steps, torch, flush) -> dict:
             "val_force_rel_err_mean": rep["val_force_rel_mean"], "val_force_rel_err_max": rep["val_force_rel_max"],
             "val_rupture_rel_err_max": rep["val_rupture_rel_max"], "rebuilds": m1["rebuilds"] - m0["rebuilds"],
             "network_evaluations_per_step": evals / args.steps,
-            "formula_fallback_fraction": falls / max(evals + falls, 1), "evaluations_per_s": rates}
+            "formula_fallback_fraction": falls / max(evals + falls, 1), "evaluations_per_s": rates,
+            "errors_vs_fp64_formula": errors, "model": LIQUID_CFG}
 
 
 def reference_kernels(w, args, flush, value, closure, kernel_ms) -> dict:

@@ -189,7 +189,12 @@ __global__ void __launch_bounds__(128) k_wall_force64(
     } else if (w == 1) {
       jp = make_double3(ip.x, ip.y, c.Bw);
     } else if (w == 2) {
-      const double dist = pow(pow((c.cir.x - ip.x), 2.0) + pow((c.cir.y - ip.y), 2.0), 0.5);
+      /* the reference's pow(pow(dx, 2) + pow(dy, 2), 0.5) (kernel.cu:1009) as the
+       * correctly rounded squares and square root it denotes: CUDA's pow has up
+       * to 2 ulp of error, and the wall overlap r - |p - jp| amplifies an error
+       * of dist by R / overlap (~10^4 here) */
+      const double ddx = c.cir.x - ip.x, ddy = c.cir.y - ip.y;
+      const double dist = sqrt(ddx * ddx + ddy * ddy);
       const double cs = (ip.x - c.cir.x) / dist;
       const double sn = (ip.y - c.cir.y) / dist;
       jp.x = c.R * cs + c.cir.x;

@@ -126,6 +126,40 @@ def _wall_ties(sim, w, s, rel, out) -> None:
         np.add.at(out, idx[t], 2.0 * pw.sfrc * fN[t])
 
 
+def wall_amplification(sim, w, ulps: float = 8.0) -> np.ndarray:
+    """Per particle, how far its force can move when its distance to the
+    cylinder axis is rounded differently (libm vs CUDA: a few ulps).  The
+    reference places a lateral-wall contact point at R (p - c) / |p - c| + c
+    (kernel.cu:1009-1013) and takes the overlap r - |p - jp|: an error e of the
+    distance moves the overlap by R e, relative R e / overlap (~10^4 ulps for a
+    1e-3 overlap at R = 12.5), and the Hertz force ~ overlap^1.5 follows it with
+    1.5 times that.  Summed over the particle's lateral-wall contacts."""
+    s = w.setup.s
+    pw, cyl = s.pwcal, s.cyl
+    n = w.setup.n
+    nw = sim.arr("nwall", np.int32, n)
+    wl = sim.arr("wlist", np.int32, 3 * n).reshape(n, 3)
+    wr = sim.wall_records()
+    reach = cyl.R + np.hypot(cyl.cir_x, cyl.cir_y)
+    out = np.zeros(n)
+    k43w = 4.0 / 3.0 * pw.emod
+    for a in range(3):
+        m = (nw > a) & (wl[:, a] == 2)
+        if not m.any():
+            continue
+        rec = wr[m, a]
+        Rw = w.setup.rad[m]
+        nrm, prad, pdfm, st = rec[:, 3], rec[:, 5], rec[:, 6], rec[:, 7]
+        with np.errstate(invalid="ignore", divide="ignore"):
+            el = k43w * np.sqrt(np.abs(Rw * nrm)) * nrm
+            pl = pw.yforce_t * Rw * Rw + pw.ystiff_t * Rw * (nrm - pw.ydsp_t * Rw)
+            un = k43w * np.sqrt(np.abs(prad)) * np.abs(nrm - pdfm) ** 1.5
+            fN = np.where(st == 2, np.where(nrm < pw.ydsp_t * Rw, el, pl), np.where(st >= 3, un, 0.0))
+            amp = np.where(nrm > 0, 1.5 * np.abs(fN) * reach * ulps * 2.0 ** -52 / nrm, 0.0)
+        np.add.at(out, np.flatnonzero(m), np.nan_to_num(amp))
+    return out
+
+
 def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: float = 0.0) -> dict:
     """Compare the GPU's post-step snapshot with the oracle's post-step state."""
     ref = sim.state()
@@ -136,12 +170,13 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
     ties = 0
     if bad.any():
         num0 = sim.arr("Num_Nebor", np.int32, n).copy()
-        budget = slip_ties(sim, w, num0, sim.history_flat())
-        # a flipped branch changes one friction force: bounded by 2 mu fN per tie contact
+        # a flipped branch changes one friction force: bounded by 2 mu fN per tie contact;
+        # last-ulp differences of the distance to the axis move lateral-wall forces
+        budget = slip_ties(sim, w, num0, sim.history_flat()) + wall_amplification(sim, w)
         aerr = np.abs(snap["force"] - ref["force"]).max(axis=1)
         over = bad & (aerr > budget * (1 + 1e-6) + tol["force"] * fscale)
-        assert not over.any(), f"{label}: force error {perr.max():.3e} not explained by slip ties at " \
-                               f"{np.flatnonzero(over)[:8]}"
+        assert not over.any(), f"{label}: force error {perr.max():.3e} not explained by slip ties or wall " \
+                               f"rounding at {np.flatnonzero(over)[:8]}"
         ties = int(bad.sum())
     ok = ~bad
     ferr = perr[ok].max() if ok.any() else 0.0
@@ -183,12 +218,18 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
     assert np.array_equal(snap["nwall"], nw), f"{label}: wall list lengths"
     wl = sim.arr("wlist", np.int32, 3 * n).reshape(n, 3)
     wr = sim.wall_records()
+    # the overlap-like fields of a lateral-wall record (nDsp, nDsp_mx, plstDfm)
+    # may move by R times a few ulps of the distance to the axis (wall_amplification)
+    slack = (w.setup.s.cyl.R + np.hypot(w.setup.s.cyl.cir_x, w.setup.s.cyl.cir_y)) * 8.0 * 2.0 ** -52
     for a in range(3):
         m = nw > a
         assert np.array_equal(snap["wlist"][m, a], wl[m, a]), f"{label}: wall list"
         if m.any():
             ws = max(np.abs(wr[m, a, :7]).max(), 1e-300)
-            werr = np.abs(snap["wrec"][m, a, :7] - wr[m, a, :7]).max() / ws
+            dif = np.abs(snap["wrec"][m, a, :7] - wr[m, a, :7])
+            lateral = (wl[m, a] == 2)[:, None] & np.isin(np.arange(7), (3, 4, 6))[None, :]
+            dif = np.where(lateral, np.maximum(dif - slack, 0.0), dif)
+            werr = dif.max() / ws
             assert werr <= tol["hist"] or (mismatch_budget > 0 and werr <= 1e3 * tol["hist"]), \
                 f"{label}: wall history error {werr:.3e}"
     return {"force_err": ferr, "hist_err": herr, "stage_mismatch": st_mis, "tie_particles": ties}
