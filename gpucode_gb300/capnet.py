@@ -92,12 +92,15 @@ class CapNet:
               "dem_capnet_grad")
         return g, float(loss.value)
 
-    def infer(self, x, tensor_cores: bool = True):
+    def infer(self, x, tensor_cores: bool | str = True):
+        """raw features -> raw outputs: tensor_cores True (or "warp") the BF16
+        warp tiles the fused step kernel runs, "tcgen05" 128-row tiles on the
+        5th-generation tensor cores, False the FP32 network"""
         import torch
 
+        mode = {True: 1, "warp": 1, "tcgen05": 2, False: 0}[tensor_cores]
         y = torch.empty((x.shape[0], 2), dtype=torch.float32, device=x.device)
-        check(self.lib.dem_capnet_infer(self.h, _dev(x), int(x.shape[0]), 1 if tensor_cores else 0, _dev(y)),
-              "dem_capnet_infer")
+        check(self.lib.dem_capnet_infer(self.h, _dev(x), int(x.shape[0]), mode, _dev(y)), "dem_capnet_infer")
         return y
 
 

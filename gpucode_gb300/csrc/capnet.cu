@@ -371,6 +371,243 @@ __global__ void __launch_bounds__(128) k_infer_tc(const CapNetSmem* __restrict__
   }
 }
 
+/* ---------------- the network on the 5th-generation tensor cores ----------------
+ * One CTA of 128 threads takes 128 bridges (one row each) at a time and runs
+ * layers 1 and 2 as tcgen05.mma (kind::f16: BF16 operands from shared memory,
+ * FP32 accumulators in tensor memory), M = 128 rows, N = 64 hidden units:
+ *   layer 1: D1[128 x 64] = X[128 x 16] W1^T   (K = 4 inputs padded to 16: one MMA)
+ *   layer 2: D2[128 x 64] = S1[128 x 64] W2^T  (K = 64: four MMAs of K = 16)
+ * Each thread reads its row of D1 / D2 back with tcgen05.ld (warp w owns
+ * tensor-memory lanes 32w..32w+31), adds the bias, applies SiLU (the same
+ * hardware-tanh form as the warp tiles), writes layer 2's BF16 operand row,
+ * and evaluates layer 3 (2 outputs) on the CUDA cores.  One thread issues the
+ * MMAs; their completion arrives on an mbarrier through tcgen05.commit.
+ *
+ * Operands are in the canonical no-swizzle K-major layout: 8-row x 16-byte
+ * core matrices, 128 bytes each; the core matrices of one 8-row group are
+ * adjacent along K (leading-dimension offset 128 B), 8-row groups follow
+ * each other (stride-dimension offset = 128 B x cores along K). */
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcCols = 128;  /* tensor-memory columns: D1 at 0, D2 at 64 */
+constexpr long long kTcSpin = 1ll << 26; /* mbarrier polls before giving up */
+
+struct __align__(128) TcSmem {
+  __nv_bfloat16 a1[kTcRows * 16];   /* X, 16 row groups x 2 K cores */
+  __nv_bfloat16 a2[kTcRows * kCapH]; /* SiLU(layer 1), 16 row groups x 8 K cores */
+  __nv_bfloat16 b1[kCapH * 16];     /* W1 [n][k], 8 n groups x 2 K cores */
+  __nv_bfloat16 b2[kCapH * kCapH];  /* W2 [n][k], 8 n groups x 8 K cores */
+  float bias1[kCapH], bias2[kCapH], w3[2][kCapH], b3[2];
+  float xm[4], xis[4], ym[2], ys[2];
+  unsigned long long mbar;
+  uint32_t tmem_base;
+};
+
+/* byte offset of element (row, k) of a K-major operand with `kcores` core
+ * matrices along K */
+__device__ __forceinline__ uint32_t tc_off(int row, int k, int kcores) {
+  return (uint32_t)((row >> 3) * (kcores * 128) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+/* shared-memory matrix descriptor: start, leading (K) and stride (8-row)
+ * byte offsets, version 1, no swizzle */
+__device__ __forceinline__ unsigned long long tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (unsigned long long)((saddr >> 4) & 0x3FFFu) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+/* instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+ * K-major, N = 64, M = 128 */
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kCapH >> 3) << 17) |
+                              ((uint32_t)(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, unsigned long long a, unsigned long long b, int acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kTcIdesc), "r"(acc));
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+/* wait for the mbarrier's phase `parity` to complete; false after kTcSpin polls */
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+  for (long long i = 0; i < kTcSpin; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tc_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+/* raw features -> raw outputs; err gets 1 if an MMA completion was not seen
+ * within kTcSpin polls (the kernel then stops; tensor memory is freed on
+ * every path) */
+__global__ void __launch_bounds__(kTcRows, 1) k_infer_tc5(const CapNetSmem* __restrict__ wsrc,
+                                                          const float* __restrict__ xr, long long n,
+                                                          float* __restrict__ y, int* __restrict__ err) {
+  __shared__ TcSmem sm;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  /* weights into the canonical layout, biases and the last layer as FP32 */
+  for (int e = tid; e < kCapH * 16; e += kTcRows) {
+    const int nn = e >> 4, k = e & 15;
+    *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(sm.b1) + tc_off(nn, k, 2)) = wsrc->w1[nn * kCapS1 + k];
+  }
+  for (int e = tid; e < kCapH * kCapH; e += kTcRows) {
+    const int nn = e >> 6, k = e & 63;
+    *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(sm.b2) + tc_off(nn, k, 8)) = wsrc->w2[nn * kCapS2 + k];
+  }
+  for (int e = tid; e < kTcRows * 16; e += kTcRows) sm.a1[e] = __float2bfloat16(0.f);
+  if (tid < kCapH) {
+    sm.bias1[tid] = wsrc->b1[tid];
+    sm.bias2[tid] = wsrc->b2[tid];
+    sm.w3[0][tid] = __bfloat162float(wsrc->w3[tid]);
+    sm.w3[1][tid] = __bfloat162float(wsrc->w3[kCapS2 + tid]);
+  }
+  if (tid < 4) {
+    sm.xm[tid] = wsrc->x_mean[tid];
+    sm.xis[tid] = wsrc->x_inv_std[tid];
+  }
+  if (tid < 2) {
+    sm.b3[tid] = wsrc->b3[tid];
+    sm.ym[tid] = wsrc->y_mean[tid];
+    sm.ys[tid] = wsrc->y_std[tid];
+  }
+  const uint32_t mbar = smem_u32(&sm.mbar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_sync();
+  const uint32_t tmem = sm.tmem_base;
+  const uint32_t d1 = tmem, d2 = tmem + (uint32_t)kCapH;
+  const uint32_t lane_base = (uint32_t)(32 * warp) << 16; /* this warp's tensor-memory lanes */
+  const unsigned long long da1 = tc_desc(smem_u32(sm.a1), 128, 2 * 128);
+  const unsigned long long db1 = tc_desc(smem_u32(sm.b1), 128, 2 * 128);
+  uint32_t parity = 0;
+  bool ok = true;
+  const long long tiles = (n + kTcRows - 1) / kTcRows;
+  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const long long row = tile * kTcRows + tid;
+    /* layer 1 operand: this row's standardised inputs (k 0..3; k 4..15 stay 0) */
+    float x0 = 0.f, x1 = 0.f, x2 = 0.f, x3 = 0.f;
+    if (row < n) {
+      const float4 f = *reinterpret_cast<const float4*>(xr + 4 * row);
+      x0 = (__logf(f.x) - sm.xm[0]) * sm.xis[0];
+      x1 = (__logf(f.y) - sm.xm[1]) * sm.xis[1];
+      x2 = (f.z - sm.xm[2]) * sm.xis[2];
+      x3 = (f.w - sm.xm[3]) * sm.xis[3];
+    }
+    {
+      uint2 v;
+      v.x = pack_bf16(x0, x1);
+      v.y = pack_bf16(x2, x3);
+      *reinterpret_cast<uint2*>(reinterpret_cast<char*>(sm.a1) + tc_off(tid, 0, 2)) = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_sync();
+    if (tid == 0) {
+      tc_mma(d1, da1, db1, 0);
+      tc_commit(mbar);
+    }
+    /* every thread polls with a bound; the block decides together */
+    ok = __syncthreads_and(tc_wait(mbar, parity)) != 0;
+    if (!ok) break;
+    parity ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    /* layer 1 out: bias, SiLU, BF16 into layer 2's operand row */
+#pragma unroll
+    for (int c = 0; c < kCapH; c += 16) {
+      float v[16];
+      tc_ld16(d1 + lane_base + (uint32_t)c, v);
+      uint4 lo, hi;
+      lo.x = pack_bf16(cap_silu(v[0] + sm.bias1[c + 0]), cap_silu(v[1] + sm.bias1[c + 1]));
+      lo.y = pack_bf16(cap_silu(v[2] + sm.bias1[c + 2]), cap_silu(v[3] + sm.bias1[c + 3]));
+      lo.z = pack_bf16(cap_silu(v[4] + sm.bias1[c + 4]), cap_silu(v[5] + sm.bias1[c + 5]));
+      lo.w = pack_bf16(cap_silu(v[6] + sm.bias1[c + 6]), cap_silu(v[7] + sm.bias1[c + 7]));
+      hi.x = pack_bf16(cap_silu(v[8] + sm.bias1[c + 8]), cap_silu(v[9] + sm.bias1[c + 9]));
+      hi.y = pack_bf16(cap_silu(v[10] + sm.bias1[c + 10]), cap_silu(v[11] + sm.bias1[c + 11]));
+      hi.z = pack_bf16(cap_silu(v[12] + sm.bias1[c + 12]), cap_silu(v[13] + sm.bias1[c + 13]));
+      hi.w = pack_bf16(cap_silu(v[14] + sm.bias1[c + 14]), cap_silu(v[15] + sm.bias1[c + 15]));
+      *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm.a2) + tc_off(tid, c, 8)) = lo;
+      *reinterpret_cast<uint4*>(reinterpret_cast<char*>(sm.a2) + tc_off(tid, c + 8, 8)) = hi;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_sync();
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < kCapH / 16; k++) {
+        const unsigned long long da = tc_desc(smem_u32(sm.a2) + 256u * k, 128, 8 * 128);
+        const unsigned long long db = tc_desc(smem_u32(sm.b2) + 256u * k, 128, 8 * 128);
+        tc_mma(d2, da, db, k > 0);
+      }
+      tc_commit(mbar);
+    }
+    ok = __syncthreads_and(tc_wait(mbar, parity)) != 0;
+    if (!ok) break;
+    parity ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    /* layer 2 out: bias, SiLU, and layer 3 on the CUDA cores */
+    float o0 = sm.b3[0], o1 = sm.b3[1];
+#pragma unroll
+    for (int c = 0; c < kCapH; c += 16) {
+      float v[16];
+      tc_ld16(d2 + lane_base + (uint32_t)c, v);
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        /* the same BF16 rounding of the activations as the warp tiles */
+        const float a = __bfloat162float(__float2bfloat16(cap_silu(v[i] + sm.bias2[c + i])));
+        o0 = fmaf(sm.w3[0][c + i], a, o0);
+        o1 = fmaf(sm.w3[1][c + i], a, o1);
+      }
+    }
+    if (row < n) {
+      y[2 * row] = o0 * sm.ys[0] + sm.ym[0];
+      y[2 * row + 1] = o1 * sm.ys[1] + sm.ym[1];
+    }
+    tc_sync(); /* every row read before the next tile's MMAs overwrite D1 / D2 */
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(err, 1);
+    /* the phase that was not seen: whatever was issued completes (bounded)
+     * before the memory is freed */
+    tc_wait(mbar, parity);
+  }
+  tc_sync();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
+  }
+}
+
 /* the plain closure on raw features: FP64 as the reference evaluates it
  * (kernel.cu:65-81 with pow/log/exp, :518), or the step kernel's FP32 form */
 __global__ void k_formula64(const float* __restrict__ xr, long long n, float* __restrict__ y, int angle) {
@@ -614,7 +851,27 @@ dem_status dem_capnet_infer(dem_capnet* net, const float* x_dev, long long n, in
   if (!net || !x_dev || !y_dev || n < 0) return fail(DEM_ERR_ARG, "dem_capnet_infer: bad arguments");
   if (!net->has_norm) return fail(DEM_ERR_STATE, "dem_capnet_infer: no standardisation");
   if (n == 0) return DEM_OK;
-  if (tensor_cores) {
+  if (tensor_cores == 2) {
+    /* the 5th-generation tensor cores: 128-row tiles, tcgen05.mma into tensor memory */
+    dem_status st = ensure_packed(net);
+    if (st != DEM_OK) return st;
+    int* err = nullptr;
+    st = cuda_alloc((void**)&err, sizeof(int));
+    if (st != DEM_OK) return st;
+    st = ck(cudaMemset(err, 0, sizeof(int)), "dem_capnet_infer");
+    const long long tiles = (n + kTcRows - 1) / kTcRows;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    const int blocks = (int)std::min<long long>(tiles, (long long)std::max(1, sms) * 4);
+    if (st == DEM_OK) k_infer_tc5<<<blocks, kTcRows>>>(net->packed, x_dev, n, y_dev, err);
+    if (st == DEM_OK) st = ck(cudaGetLastError(), "dem_capnet_infer launch");
+    if (st == DEM_OK) st = ck(cudaDeviceSynchronize(), "dem_capnet_infer");
+    int h = 0;
+    if (st == DEM_OK) st = ck(cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost), "dem_capnet_infer");
+    cudaFree(err);
+    if (st == DEM_OK && h) st = fail(DEM_ERR_CUDA, "dem_capnet_infer: tensor-core completion not seen in time");
+    return st;
+  } else if (tensor_cores) {
     dem_status st = ensure_packed(net);
     if (st != DEM_OK) return st;
     const long long tiles = (n + 15) / 16;

@@ -568,8 +568,10 @@ dem_status dem_capnet_fit(dem_capnet* net, const float* x_dev, const float* y_de
  * standardised outputs) with respect to the 4610 parameters, and the loss. */
 dem_status dem_capnet_grad(dem_capnet* net, const float* x_dev, const float* y_dev, int n, float* grad,
                            float* loss);
-/* Raw features -> raw outputs: tensor_cores = 1 runs the BF16 tiles the step
- * kernel uses, 0 the FP32 network. */
+/* Raw features -> raw outputs: tensor_cores = 1 runs the BF16 warp tiles the
+ * step kernel uses (mma.sync, 16 rows per warp), 2 the same network on the
+ * 5th-generation tensor cores (tcgen05.mma into tensor memory, 128 rows per
+ * CTA), 0 the FP32 network. */
 dem_status dem_capnet_infer(dem_capnet* net, const float* x_dev, long long n, int tensor_cores, float* y_dev);
 /* The plain closure the network stands in for, on the same raw features:
  * bit 0 of fp64 set: FP64 as the reference evaluates it (FP64 pow/log/exp),

@@ -160,6 +160,29 @@ def wall_amplification(sim, w, ulps: float = 8.0) -> np.ndarray:
     return out
 
 
+def bridge_flips(sim, w, snap, num, hist) -> np.ndarray:
+    """Per particle, the capillary forces of its bridges whose flag the GPU set
+    differently from the oracle: a bridge forms below a gap threshold and
+    ruptures above another (kernel.cu:518-521), so where FP32 and FP64 round a
+    gap on either side of one, the whole bridge force (at most 2 pi R_eff
+    gamma: the regression's F* stays below 1) appears on one side only.  Only
+    where the lists agree (else the list check reports them)."""
+    out = np.zeros(w.setup.n)
+    if not np.array_equal(snap["counts"], num):
+        return out
+    _, flat = sim.lists_flat()
+    if len(flat) != len(snap["brg"]) or not np.array_equal(snap["partners"], flat):
+        return out
+    flip = np.asarray(snap["brg"]) != hist[:, 8]
+    if not flip.any():
+        return out
+    ii, _, _ = sim.slots_of(num)
+    jj = flat.astype(np.int64)
+    ri, rj = w.setup.rad[ii[flip]], w.setup.rad[jj[flip]]
+    np.add.at(out, ii[flip], 2.0 * np.pi * (2.0 * ri * rj / (ri + rj)) * w.setup.s.lqd.stension)
+    return out
+
+
 def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: float = 0.0) -> dict:
     """Compare the GPU's post-step snapshot with the oracle's post-step state."""
     ref = sim.state()
@@ -172,11 +195,14 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
         num0 = sim.arr("Num_Nebor", np.int32, n).copy()
         # a flipped branch changes one friction force: bounded by 2 mu fN per tie contact;
         # last-ulp differences of the distance to the axis move lateral-wall forces
-        budget = slip_ties(sim, w, num0, sim.history_flat()) + wall_amplification(sim, w)
+        hist0 = sim.history_flat()
+        budget = slip_ties(sim, w, num0, hist0) + wall_amplification(sim, w)
+        if mismatch_budget > 0:
+            budget += bridge_flips(sim, w, snap, num0, hist0)
         aerr = np.abs(snap["force"] - ref["force"]).max(axis=1)
         over = bad & (aerr > budget * (1 + 1e-6) + tol["force"] * fscale)
-        assert not over.any(), f"{label}: force error {perr.max():.3e} not explained by slip ties or wall " \
-                               f"rounding at {np.flatnonzero(over)[:8]}"
+        assert not over.any(), f"{label}: force error {perr.max():.3e} not explained by slip ties, wall " \
+                               f"rounding or bridge flips at {np.flatnonzero(over)[:8]}"
         ties = int(bad.sum())
     ok = ~bad
     ferr = perr[ok].max() if ok.any() else 0.0
@@ -201,6 +227,9 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
         f"{label}: stage mismatch {st_mis:.3e}, bridge mismatch {br_mis:.3e}"
     same = (got[:, 7] == hist[:, 7])
     hs = np.maximum(np.abs(hist[:, :7]).max(axis=0), 1e-300) if len(hist) else np.ones(7)
+    # plstDfm = overlap - (fN / k)^(2/3) (kernel.cu:128): a difference of two
+    # near-equal terms, so its rounding is relative to the overlap's scale
+    hs[6] = max(hs[6], hs[3])
     rel = np.abs(got[:, :7] - hist[:, :7]) / hs
     herr = rel[same].max() if same.any() else 0.0
     if herr > tol["hist"]:
@@ -212,7 +241,10 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
         excused[spring_ok, 0:3] = True
         left = rel[same[:, None] & ~excused] if len(rel) else np.zeros(0)
         herr = float(left.max()) if left.size else 0.0
-    assert herr <= tol["hist"], f"{label}: history error {herr:.3e}"
+    if herr > tol["hist"]:
+        col = int(np.argmax((rel * same[:, None]).max(axis=0)))
+        raise AssertionError(f"{label}: history error {herr:.3e} (column {col} of dispt xyz, nDsp, nDsp_mx, "
+                             "plstRad, plstDfm)")
     assert np.array_equal(snap["lqd"], sim.arr("lqdCnt", np.int32, n)) or mismatch_budget > 0, f"{label}: lqd"
     nw = sim.arr("nwall", np.int32, n)
     assert np.array_equal(snap["nwall"], nw), f"{label}: wall list lengths"

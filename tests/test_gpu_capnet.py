@@ -74,6 +74,14 @@ def test_inference_matches_the_oracle(cuda):
     # ragged tail: a count that is not a multiple of the 16-row tile
     got_t = net.infer(_t(x[:37]), tensor_cores=True).cpu().numpy()
     np.testing.assert_array_equal(got_t, got[:37])
+    # the same network on the 5th-generation tensor cores (tcgen05.mma, 128-row
+    # tiles; 5000 rows leave a ragged last tile): the same BF16 rounding points
+    got5 = net.infer(_t(x), tensor_cores="tcgen05").cpu().numpy()
+    d5 = np.abs(got5 - emul) / ys
+    assert d5.max() < 2e-2 and d5.mean() < 2e-3, (d5.max(), d5.mean())
+    assert (np.abs(got5 - got) / ys).mean() < 1e-3
+    got5_t = net.infer(_t(x[:37]), tensor_cores="tcgen05").cpu().numpy()
+    np.testing.assert_array_equal(got5_t, got5[:37])
     net.close()
 
 
@@ -140,15 +148,21 @@ def test_training_learns_the_closure(trained):
     fresh.close()
 
 
-def test_network_gains_over_the_reference_precision_formula(trained):
-    """the trained network on the tensor cores against the plain closure as the
-    reference evaluates it (FP64 pow/log/exp): same inputs, time per bridge"""
+def test_network_against_the_formulas(trained):
+    """The trained network against the plain closure it stands in for, per
+    bridge on the same inputs: the formula as the reference evaluates it (FP64
+    pow/log/exp) and the FP32 form the fast step kernel runs.  The network (on
+    either tensor-core path) is faster than the FP64 formula and within 5 % of
+    it on average; the FP32 formula is closer to the FP64 one than the network
+    is: on this GPU the closed form costs a handful of hardware log/exp per
+    bridge where the network's 128 SiLU activations alone take longer, so the
+    FP32 formula is what the fast path runs."""
     import torch
 
     net, _, x, _ = trained
     big = x.repeat((2_000_000 // len(x)) + 1, 1)[:2_000_000].contiguous()
-    y_tc = net.infer(big, tensor_cores=True)
     y_64 = capnet.formula(big, fp64=True)
+    y_32 = capnet.formula(big, fp64=False)
 
     def timed(fn, reps=5):
         fn()
@@ -161,11 +175,16 @@ def test_network_gains_over_the_reference_precision_formula(trained):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
-    t_tc = timed(lambda: net.infer(big, tensor_cores=True))
+    def rel(y):
+        return (torch.abs(y[:, 0] - y_64[:, 0]) / torch.abs(y_64[:, 0])).mean().item()
+
     t_64 = timed(lambda: capnet.formula(big, fp64=True))
-    assert t_tc < 0.5 * t_64, (t_tc, t_64)
-    rel = (torch.abs(y_tc[:, 0] - y_64[:, 0]) / torch.abs(y_64[:, 0])).mean().item()
-    assert rel < 0.05
+    for mode in (True, "tcgen05"):
+        y = net.infer(big, tensor_cores=mode)
+        assert timed(lambda: net.infer(big, tensor_cores=mode)) < 0.5 * t_64, mode
+        assert rel(y) < 0.05, mode
+        assert rel(y_32) < rel(y), (mode, rel(y_32), rel(y))
+    assert rel(y_32) < 1e-5
 
 
 @pytest.mark.parametrize("pairs", ["warp", "thread"])
