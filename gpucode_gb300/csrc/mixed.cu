@@ -134,6 +134,17 @@ struct KSum3 {
   KSum x, y, z;
   __device__ __forceinline__ void add(float3 v) { x.add(v.x); y.add(v.y); z.add(v.z); }
 };
+/* four Kahan sums kept as (sums, compensations) in two float4s of shared memory */
+__device__ __forceinline__ void kahan4(float4* acc, float3 v, float w) {
+  float4 sm = acc[0], cm = acc[1];
+  KSum t;
+  t.s = sm.x; t.c = cm.x; t.add(v.x); sm.x = t.s; cm.x = t.c;
+  t.s = sm.y; t.c = cm.y; t.add(v.y); sm.y = t.s; cm.y = t.c;
+  t.s = sm.z; t.c = cm.z; t.add(v.z); sm.z = t.s; cm.z = t.c;
+  t.s = sm.w; t.c = cm.w; t.add(w); sm.w = t.s; cm.w = t.c;
+  acc[0] = sm;
+  acc[1] = cm;
+}
 
 /* error-free transforms (Knuth two-sum, FMA two-product) */
 __device__ __forceinline__ float two_sum(float a, float b, float& err) {
@@ -586,8 +597,15 @@ __device__ __forceinline__ void finish_particle(const MixArgs& a, int q, int qq,
   }
 }
 
+/* resident blocks per SM the thread loop is built for: 6 (80 registers, a few
+ * bytes of spills; its moment sums live in shared memory) measured 5 % faster
+ * on the packed 200k wet bed than 5 (96 registers); 7 spills more and is slower */
+#ifndef DEM_MIXED_BLOCKS
+#define DEM_MIXED_BLOCKS 6
+#endif
+
 template <bool WET, bool NET>
-__global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArgs a) {
+__global__ void __launch_bounds__(128, NET ? kNetBlocks : DEM_MIXED_BLOCKS) k_step_mixed(MixArgs a) {
   if (a.n <= 0 || (a.gate && *a.gate)) return;
   const int q = reversed_block_thread(); /* the heaviest particles first */
   const bool live = q < a.n;
@@ -616,9 +634,14 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
   const float3 iv = f3(vi4.x, vi4.y, vi4.z), iw = f3(wi4.x, wi4.y, wi4.z);
   const float twor = 2.0f * ri;
   const float mass_f = twor * twor * twor;
-  KSum3 F, M;
-  KSum R;
+  KSum3 F;
   F.z.add(-mass_f); /* gravity, m = (2r)^3 */
+  /* the moment and rolling-moment Kahan sums (sum, compensation) wait in
+   * shared memory while the pairs are evaluated: registers for the pair loop */
+  __shared__ float4 mr_acc[2 * 128];
+  float4* const mra = mr_acc + 2 * threadIdx.x;
+  mra[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+  mra[1] = make_float4(0.f, 0.f, 0.f, 0.f);
   int wet = 0;
   float iVol = 0.f;
   /* batched systems: this particle's system (its cylinder, dry or wet) */
@@ -683,8 +706,7 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
         float dR;
         pp_contact(a.pp, a.rec + s, ri, rj, iv, iw, vj4, ro(a.w_in + j), u, gap, a.rfrc, a.dtf, dF, dM, dR);
         F.add(dF);
-        M.add(dM);
-        R.add(dR);
+        kahan4(mra, dM, dR);
         ncont++;
       }
     }
@@ -761,6 +783,13 @@ __global__ void __launch_bounds__(128, NET ? kNetBlocks : 5) k_step_mixed(MixArg
   }
   if (NET && qn > 0) cap_flush(*capw, qw, qn, last, a.brg, F, wet, nbr, nmlp);
 
+  KSum3 M;
+  KSum R;
+  {
+    const float4 sm = mra[0], cm = mra[1];
+    M.x.s = sm.x; M.x.c = cm.x; M.y.s = sm.y; M.y.c = cm.y; M.z.s = sm.z; M.z.c = cm.z;
+    R.s = sm.w; R.c = cm.w;
+  }
   finish_particle<NET>(a, q, qq, live, sys, hi, lo, wi4, iv, iw, ri, twor, mass_f, F, M, R, wet, (unsigned)nn, ncont,
                        nbr, nmlp, nfall);
 }
@@ -1360,10 +1389,7 @@ Prefilter mixed_prefilter(dem_ctx* c, int which) {
   return Prefilter{c->mx->phi[which], 0.5f * c->mx->coarse_tol + 2.0e-6f};
 }
 
-bool mixed_thread_loop(const dem_ctx* c) {
-  const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;
-  return c->opt.pair_mode == DEM_PAIRS_THREAD || (c->opt.pair_mode == DEM_PAIRS_AUTO && net);
-}
+bool mixed_thread_loop(const dem_ctx* c) { return c->opt.pair_mode != DEM_PAIRS_WARP; }
 
 const char* mixed_step_kernel_name(const dem_ctx* c) {
   const bool net = c->s.force_cap == 1 && c->opt.capillary == DEM_CAP_MLP;

@@ -187,6 +187,9 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
     """Compare the GPU's post-step snapshot with the oracle's post-step state."""
     ref = sim.state()
     n = w.setup.n
+    # how near its slip limit a spring counts as a tie: FP64 on both sides
+    # rounds within 1e-9 of it; the mixed path keeps the spring's FP32 copy
+    tie_rel = 1e-9 if mismatch_budget == 0 else 1e-5
     fscale = max(np.abs(ref["force"]).max(), 1e-300)
     perr = np.abs(snap["force"] - ref["force"]).max(axis=1) / fscale
     bad = perr > tol["force"]
@@ -196,7 +199,7 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
         # a flipped branch changes one friction force: bounded by 2 mu fN per tie contact;
         # last-ulp differences of the distance to the axis move lateral-wall forces
         hist0 = sim.history_flat()
-        budget = slip_ties(sim, w, num0, hist0) + wall_amplification(sim, w)
+        budget = slip_ties(sim, w, num0, hist0, rel=tie_rel) + wall_amplification(sim, w)
         if mismatch_budget > 0:
             budget += bridge_flips(sim, w, snap, num0, hist0)
         aerr = np.abs(snap["force"] - ref["force"]).max(axis=1)
@@ -235,7 +238,7 @@ def compare_step(snap: dict, sim, w, tol: dict, label: str, mismatch_budget: flo
     if herr > tol["hist"]:
         # the spring (columns 0-2) of a tie contact legitimately differs (slip
         # rescale vs stick); nothing else of it, and nothing of other contacts
-        _, tie = slip_ties(sim, w, num, hist, contacts=True)
+        _, tie = slip_ties(sim, w, num, hist, rel=tie_rel, contacts=True)
         spring_ok = same & tie
         excused = np.zeros_like(rel, dtype=bool)
         excused[spring_ok, 0:3] = True
