@@ -45,6 +45,9 @@ METRIC = "particle-steps/s, 200k wet spheres, vs FP64 plain; packing-frac & Z er
 UNIT = "particle-steps/s"
 BED = ROOT / "tests" / "golden" / "packed_wet200k.npz"
 DATA = "synthetic (seeded log-normal sizes, packed bed from tests/golden/packed_wet200k.npz)"
+# the configured liquid: bridge volume per contact uniform in [0.5 %, 2 %] of the
+# smaller sphere's volume, contact angle per particle uniform in [0, 30 deg]
+LIQUID_CFG = {"vol_min": 0.005, "vol_max": 0.02, "theta_max": 0.5235987755982988, "seed": 2}
 
 
 def bed_config(w) -> dict:
@@ -329,9 +332,10 @@ def run_ensemble(args):
 
 def train_closure(samples: int, epochs: int, settle: int = 2000, snaps: int = 11):
     """The learned capillary closure as the wet workloads deploy it: samples of
-    the plain formula logged from the 200,000-sphere wet bed while it settles
-    (`snaps` points spread over `settle` steps), then trained on the GPU by the
-    library's own kernels (seeded 90/10 split, Adam lr 1e-3, batch 8192).
+    the plain formula (the configured per-contact liquid, contact-angle terms
+    included) logged from the packed 200,000-sphere wet bed over `settle`
+    steps (`snaps` points), then trained on the GPU by the library's own
+    kernels (seeded 90/10 split, Adam lr 1e-3, batch 8192).
     Returns (network, fit report, samples used)."""
     import torch
 
@@ -339,8 +343,9 @@ def train_closure(samples: int, epochs: int, settle: int = 2000, snaps: int = 11
     from gpucode_gb300 import configs
     from gpucode_gb300.engine import Engine
 
-    w = configs.wet()
+    w = configs.load_bed(BED)
     e = Engine(w.setup, precision="mixed")
+    e.set_liquid_model("per_contact", **LIQUID_CFG)
     e.set_state(w.pos0_reduced)
     per = -(-samples // snaps)
     xs, ys = [], []
@@ -407,15 +412,16 @@ def closure_error(e, net, capacity: int = 8_000_000) -> dict:
 
 def run_wet_full(args):
     """The 200,000-sphere wet packing run whole (50,000 steps of 5e-7 s) three
-    ways from the same deposited bed: FP32 forces / FP64 state with the plain
-    capillary formula, the same with the learned closure fused in the step
-    kernel, and the all-FP64 engine (the reference's formulas).  Packing
-    fraction and coordination number at checkpoints along the run; the error
-    of each fast path against the FP64 run at the end."""
+    ways from the same packed bed, with the configured per-contact liquid:
+    FP32 forces / FP64 state with the plain capillary formula, the same with
+    the learned closure fused in the step kernel, and the all-FP64 engine (the
+    reference's formulas with the contact-angle terms).  Packing fraction and
+    coordination number at checkpoints along the run; the error of each fast
+    path against the FP64 run at the end."""
     from gpucode_gb300 import configs
     from gpucode_gb300.engine import Engine, packing_metrics
 
-    w = configs.wet()
+    w = configs.load_bed(BED)
     n, total = w.setup.n, args.full_steps
     every = max(1, total // 5)
     net, rep, used = train_closure(args.capnet_samples, args.capnet_epochs)
@@ -425,6 +431,7 @@ def run_wet_full(args):
         e = Engine(w.setup, precision=prec, capillary=cap)
         if cap == "mlp":
             e.set_capnet(net)
+        e.set_liquid_model("per_contact", **LIQUID_CFG)
         e.set_state(w.pos0_reduced)
         done, wall, marks, clocks = 0, 0.0, [], []
         while done < total:
@@ -452,7 +459,7 @@ def run_wet_full(args):
         runs[name]["speedup_vs_fp64"] = runs[name]["particle_steps_per_s"] / runs["fp64"]["particle_steps_per_s"]
     print(json.dumps({
         "metric": METRIC, "workload": "wet200k-full", "unit": UNIT, "particles": n, "steps": total, "dt_s": 5e-7,
-        "data": "synthetic (seeded deposited bed, log-normal sizes)",
+        "data": DATA, "liquid": LIQUID_CFG,
         "timing": "host wall time around graph-replayed spans of steps, rebuilds included, metrics outside",
         "closure_training": {"samples": used, "epochs": rep["epochs"], "fit_seconds": rep["seconds"],
                              "val_force_rel_err_mean": rep["val_force_rel_mean"],
@@ -502,6 +509,7 @@ def run_wet_large(args, which: str):
         e = Engine(w.setup, precision="mixed", capillary=cap)
         if cap == "mlp":
             e.set_capnet(net)
+        e.set_liquid_model("per_contact", **LIQUID_CFG)
         e.set_state(w.pos0_reduced)
         e.step(16)
         s0 = e.stats()
@@ -540,6 +548,7 @@ def run_wet_large(args, which: str):
             e = Engine(ws_.setup, precision=prec, capillary=cap)
             if cap == "mlp":
                 e.set_capnet(net)
+            e.set_liquid_model("per_contact", **LIQUID_CFG)
             e.set_state(ws_.pos0_reduced)
             dt, _ = run_span(e, steps)
             m = packing_metrics(ws_.setup, e.get_state()["pos"])
@@ -926,11 +935,6 @@ def accuracy_runs(w, args, torch) -> dict:
                 o[f"max_position_diff_{name}"] = float(np.abs(runs[key] - po).max())
         out["oracle"] = o
     return out
-
-
-# the configured liquid: bridge volume per contact uniform in [0.5 %, 2 %] of the
-# smaller sphere's volume, contact angle per particle uniform in [0, 30 deg]
-LIQUID_CFG = {"vol_min": 0.005, "vol_max": 0.02, "theta_max": 0.5235987755982988, "seed": 2}
 
 
 def per_contact_liquid(w, args, timed_steps, flush) -> dict:

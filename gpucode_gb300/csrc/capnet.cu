@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(128) k_infer_tc(const CapNetSmem* __restrict__
  * each other (stride-dimension offset = 128 B x cores along K). */
 constexpr int kTcRows = 128;
 constexpr uint32_t kTcCols = 128;  /* tensor-memory columns: D1 at 0, D2 at 64 */
-constexpr long long kTcSpin = 1ll << 26; /* mbarrier polls before giving up */
+constexpr unsigned long long kTcWaitNs = 1000000000ull; /* give up on an MMA completion after 1 s */
 
 struct __align__(128) TcSmem {
   __nv_bfloat16 a1[kTcRows * 16];   /* X, 16 row groups x 2 K cores */
@@ -432,9 +432,15 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
                : "memory");
 }
-/* wait for the mbarrier's phase `parity` to complete; false after kTcSpin polls */
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+/* wait for the mbarrier's phase `parity` to complete; false after kTcWaitNs */
 __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
-  for (long long i = 0; i < kTcSpin; i++) {
+  const unsigned long long t0 = global_ns();
+  for (;;) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -442,8 +448,8 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
         : "r"(mbar), "r"(parity)
         : "memory");
     if (done) return true;
+    if (global_ns() - t0 > kTcWaitNs) return false;
   }
-  return false;
 }
 __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
@@ -463,8 +469,8 @@ __device__ __forceinline__ void tc_sync() {
 }
 
 /* raw features -> raw outputs; err gets 1 if an MMA completion was not seen
- * within kTcSpin polls (the kernel then stops; tensor memory is freed on
- * every path) */
+ * within kTcWaitNs (the kernel then stops; tensor memory is freed on every
+ * path) */
 __global__ void __launch_bounds__(kTcRows, 1) k_infer_tc5(const CapNetSmem* __restrict__ wsrc,
                                                           const float* __restrict__ xr, long long n,
                                                           float* __restrict__ y, int* __restrict__ err) {

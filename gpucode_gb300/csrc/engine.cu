@@ -846,17 +846,19 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
   if (e == cudaSuccess) e = cudaEventRecord(c->xev[0], c->stream);
   if (e == cudaSuccess && c->trace) e = cudaEventRecord(c->trace[1], c->stream);
   if (e != cudaSuccess) return cuda_check(e, "dem_set_state upload");
-  k_import<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_pos, b.tmp_vel, b.tmp_angv, b.pos, b.vel,
-                                                         b.angv, vel != nullptr, angvel != nullptr);
+  if (!request_rebuild && c->opt.precision == DEM_PREC_MIXED) {
+    /* the neighbours read the shadow copy: the import refreshes it from the
+     * new state in the same pass */
+    dem_status st = mixed_import(c, c->parity, vel != nullptr, angvel != nullptr, c->stream);
+    if (st != DEM_OK) return st;
+  } else {
+    k_import<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_pos, b.tmp_vel, b.tmp_angv, b.pos,
+                                                           b.vel, b.angv, vel != nullptr, angvel != nullptr);
+  }
   if (request_rebuild) {
     const int one = 1;
     e = cudaMemcpyAsync(b.need, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_check(e, "dem_set_state");
-  } else if (c->opt.precision == DEM_PREC_MIXED) {
-    /* the neighbours read the shadow copy: refresh it from the new state */
-    dem_status st = mixed_pre_rebuild(c, c->parity, c->stream);
-    if (st == DEM_OK) st = mixed_shadows(c, c->parity, c->stream);
-    if (st != DEM_OK) return st;
   }
   if (c->trace) cudaEventRecord(c->trace[2], c->stream);
   /* the caller's arrays are free again once the copies are done; the import

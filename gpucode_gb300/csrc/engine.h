@@ -143,6 +143,10 @@ dem_status mixed_shadows(dem_ctx* c, int which, cudaStream_t s);
 Prefilter mixed_prefilter(dem_ctx* c, int which);
 /* one fused step reading shadows `which`, writing shadows 1 - which */
 dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s);
+/* a state import without a rebuild request: the host arrays already in the
+ * tmp buffers, gathered into cell order with the shadow buffer `which`
+ * rewritten, in one launch */
+dem_status mixed_import(dem_ctx* c, int which, int has_v, int has_w, cudaStream_t s);
 /* the mixed step's pair loop: one thread per particle (true) or warp-cooperative */
 bool mixed_thread_loop(const dem_ctx* c);
 /* the name of the step kernel mixed_step launches, e.g. "k_step_mixed<1,0>" */

@@ -1287,6 +1287,40 @@ __global__ void k_shadows(int n, const double3* __restrict__ pos, const double3*
   w4[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
 }
 
+/* A state import without a rebuild in one pass: the caller-order arrays
+ * gathered into cell order (k_import), the bridge counts of the last step
+ * taken from the shadow (k_lqd_from_shadow) and the shadow rewritten from the
+ * new state (k_shadows) -- the same values as those three launches */
+__global__ void k_import_shadows(int n, const int* __restrict__ id, const double3* __restrict__ hp,
+                                 const double3* __restrict__ hv, const double3* __restrict__ hw, int has_v, int has_w,
+                                 double3* __restrict__ pos, double3* __restrict__ vel, double3* __restrict__ angv,
+                                 const double* __restrict__ rad, int* __restrict__ lqd, double3 off, int bin_exp,
+                                 float lo_scale, float4* __restrict__ phi, float4* __restrict__ plo,
+                                 float4* __restrict__ v4, float4* __restrict__ w4) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = id[q];
+  const double3 p = hp[i];
+  const double3 v = has_v ? hv[i] : make_double3(0.0, 0.0, 0.0);
+  const double3 w = has_w ? hw[i] : make_double3(0.0, 0.0, 0.0);
+  pos[q] = p;
+  vel[q] = v;
+  angv[q] = w;
+  const int lq = __float_as_int(v4[q].w);
+  lqd[q] = lq;
+  float4 ph, pl;
+  split_hi_lo(p.x + off.x, bin_exp, lo_scale, ph.x, pl.x);
+  split_hi_lo(p.y + off.y, bin_exp, lo_scale, ph.y, pl.y);
+  split_hi_lo(p.z + off.z, bin_exp, lo_scale, ph.z, pl.z);
+  const double r = rad[q];
+  ph.w = (float)r;
+  pl.w = (float)(r - (double)ph.w);
+  phi[q] = ph;
+  plo[q] = pl;
+  v4[q] = make_float4(d2f(v.x), d2f(v.y), d2f(v.z), __int_as_float(lq));
+  w4[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
+}
+
 __global__ void k_force_out(int n, const float4* __restrict__ f, double3* __restrict__ force, double3* __restrict__ mom) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -1380,6 +1414,16 @@ dem_status mixed_shadows(dem_ctx* c, int which, cudaStream_t s) {
                                                  m->lo_scale, m->phi[which],
                                                  m->plo[which], m->vel[which], m->angv[which]);
   return cuda_check(cudaGetLastError(), "mixed_shadows launch");
+}
+
+dem_status mixed_import(dem_ctx* c, int which, int has_v, int has_w, cudaStream_t s) {
+  MixedState* m = c->mx;
+  EngineBufs& b = c->b;
+  k_import_shadows<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, b.id, b.tmp_pos, b.tmp_vel, b.tmp_angv, has_v, has_w,
+                                                        b.pos, b.vel, b.angv, b.rad, b.lqd, m->off, m->bin_exp,
+                                                        m->lo_scale, m->phi[which], m->plo[which], m->vel[which],
+                                                        m->angv[which]);
+  return cuda_check(cudaGetLastError(), "mixed_import launch");
 }
 
 Prefilter mixed_prefilter(dem_ctx* c, int which) {

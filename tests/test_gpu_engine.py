@@ -208,6 +208,33 @@ def test_checkpoint_resume_is_bit_exact(cuda, tmp_path, precision):
     assert (x.value, y.value, z.value) == (w.setup.n, 3, w.setup.n)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_state_round_trip_without_rebuild_is_bit_exact(cuda, precision):
+    """dem_get_state then dem_set_state_ex(..., request_rebuild = 0) with the same
+    arrays (the end-to-end path: the import gathers into cell order and, in
+    mixed precision, rewrites the shadows and bridge counts in one pass) leaves
+    the run as if it had not been interrupted"""
+    w = _workloads.small_wet()
+    pos, vel, ang = _workloads.stirred(w)
+    a = Engine(w.setup, precision=precision)
+    b = Engine(w.setup, precision=precision)
+    for e in (a, b):
+        e.set_state(pos, vel, ang)
+        e.step(37)
+    st = b.get_state()
+    p, v, g = (np.ascontiguousarray(st[k]) for k in ("pos", "vel", "angvel"))
+    for _ in range(3):
+        _abi.check(b.lib.dem_set_state_ex(b.h, _abi.ptr(p), _abi.ptr(v), _abi.ptr(g), 0), "dem_set_state_ex")
+        b.step(9)
+        a.step(9)
+        st = b.get_state()
+        p, v, g = (np.ascontiguousarray(st[k]) for k in ("pos", "vel", "angvel"))
+    sa, sb = a.get_state(), b.get_state()
+    for k in ("pos", "vel", "angvel", "force"):
+        assert np.array_equal(sa[k], sb[k]), k
+    assert a.stats()["rebuilds"] == b.stats()["rebuilds"]
+
+
 def test_slot_overflow_is_reported_not_written(cuda):
     """A level whose slot capacity is too small: the build stops at capacity and
     dem_sync reports DEM_ERR_OVERFLOW (the reference would write past the end)."""

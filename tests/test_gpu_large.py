@@ -186,8 +186,10 @@ def test_dry_lattice_whole_run_matches_the_oracle(cuda):
     # The lattice falls freely but for the pairs its jitter starts overlapping:
     # they push apart and a few collide on; those few-body collisions are
     # chaotic (last-ulp pow differences grow), the free fall is not.
-    for k in ("fp64", "mixed"):
-        assert np.mean(dev[k] > 1e-9) < 0.05, info
+    # (mixed: every particle differs from the oracle by the FP32 rounding of
+    # its gravity increments, ~1e-7 relative; the colliding few by more)
+    for k, t in (("fp64", 1e-9), ("mixed", 1e-5)):
+        assert np.mean(dev[k] > t) < 0.05, info
     # FP64: packing fraction, coordination number and checksum of the same formulas
     assert abs(m["fp64"]["phi"] - m["oracle"]["phi"]) <= 1e-7 * m["oracle"]["phi"], info
     assert abs(m["fp64"]["z"] - m["oracle"]["z"]) <= 2.0 / m["oracle"]["n_probe"], info
