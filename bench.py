@@ -379,8 +379,9 @@ def run_span(e, steps: int) -> tuple[float, dict]:
 
 
 def closure_error(e, net, capacity: int = 8_000_000) -> dict:
-    """per-contact error of the network against the plain formula (FP64, as
-    the reference evaluates it) over every bridge of engine e's current bed"""
+    """per-contact error of the network against the plain formula it learned
+    (FP64, the per-contact liquid model's regression with its contact-angle
+    terms) over every bridge of engine e's current bed"""
     import torch
 
     from gpucode_gb300 import capnet as cn
@@ -399,7 +400,7 @@ def closure_error(e, net, capacity: int = 8_000_000) -> dict:
     if len(x) == 0:
         return {"bridges": n_all, "outside_training_box": n_all}
     yn = net.infer(x, True).double()
-    yf = cn.formula(x, True).double()
+    yf = cn.formula(x, True, angle=True).double()
     fe = (yn[:, 0] - yf[:, 0]).abs() / yf[:, 0].abs().clamp_min(1e-30)
     re = (yn[:, 1] - yf[:, 1]).abs() / yf[:, 1].abs().clamp_min(1e-30)
     q = torch.tensor([0.5, 0.99, 0.999], dtype=torch.float64, device=fe.device)
@@ -564,7 +565,7 @@ def run_wet_large(args, which: str):
         "data": "synthetic (seeded deposited bed, log-normal sizes)", "generate_s": t_gen,
         "timing": "host wall time around one graph-replayed span of steps after 16 warm-up, rebuilds included",
         "closure_training": {"samples": used, "epochs": rep["epochs"], "fit_seconds": rep["seconds"],
-                             "bed": "200,000-sphere wet bed while settling"},
+                             "bed": "the packed 200,000-sphere wet bed, per-contact liquid, 2,000 steps"},
         "memory_plan": fit, "runs": out, "sub_cylinder_vs_fp64": sub}), flush=True)
 
 

@@ -1489,13 +1489,13 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s) {
   if (net && !c->cap_w) return fail(DEM_ERR_STATE, "DEM_CAP_MLP: no network installed (dem_set_capnet)");
   const bool thread_loop = mixed_thread_loop(c);
   /* threads per block: the option (a multiple of 32 up to 128), else the
-   * fastest measured on the 200k wet bed: one warp for the warp-cooperative
-   * loop (a block frees its slot as soon as its only warp is done; 75.0 vs
-   * 79.5 us at 128 threads), two for the thread loop with the formula (81.5
-   * vs 83.5 us), four with the learned closure, whose weights are staged
-   * once per block */
+   * fastest measured: one warp for the warp-cooperative loop (a block frees
+   * its slot as soon as its only warp is done; 75.0 vs 79.5 us at 128 threads
+   * on the deposited 200k bed), four for the thread loop (118.9 vs 121.6 us
+   * at 64 and 32 threads on the packed 200k bed) and with the learned
+   * closure, whose weights are staged once per block */
   const int ob = c->opt.block_size;
-  const int bs = (ob >= 32 && ob <= 32 * kWarps && ob % 32 == 0) ? ob : net ? 32 * kWarps : thread_loop ? 64 : 32;
+  const int bs = (ob >= 32 && ob <= 32 * kWarps && ob % 32 == 0) ? ob : (net || thread_loop) ? 32 * kWarps : 32;
   const int g = grid_for(c->n, bs);
   if (c->moving_walls) {
     k_move_walls<<<1, 32, 0, s>>>(b.cyl, b.n_sys > 0 ? b.n_sys : 1, c->s.prm.dt, c->step_gate);
