@@ -574,9 +574,10 @@ CELL_SORT = ("k_hash_count", "k_tile_sums", "k_scan_tiles", "k_cell_ranges", "k_
 
 def kernel_bytes_per_particle() -> dict:
     """DRAM bytes per particle of each kernel of a rebuild + step, from the
-    committed ncu table of the 200,000-sphere bed (MB per launch / 200,000);
-    the cell sort's launches summed under the group name the library reports"""
-    p = ROOT / "profiles" / "launches_wet200k.md"
+    committed ncu table of the deposited 200,000-sphere bed (MB per launch /
+    200,000; the large beds are deposited too); the cell sort's launches summed
+    under the group name the library reports"""
+    p = ROOT / "profiles" / "launches_deposit200k.md"
     out = {}
     if not p.exists():
         return out
@@ -607,8 +608,11 @@ def kernel_table(e, n: int) -> list:
 
 
 def traffic_from_profiles(kernel: str) -> float | None:
-    """DRAM bytes per launch of the fused step kernel from the committed ncu summary."""
-    name = "step_mixed_wet200k.md" if kernel.startswith("k_step_mixed") else "step_coop_wet200k.md"
+    """DRAM bytes per launch of the fused step kernel on the packed bed, from the
+    committed ncu summary of the same kernel (None for a kernel without one)"""
+    name = {"k_step_mixed<1,0>": "step_mixed_packed200k.md"}.get(kernel)
+    if name is None:
+        return None
     p = ROOT / "profiles" / name
     if not p.exists():
         return None
@@ -779,6 +783,10 @@ def run_headline(args, ws, rank):
     accuracy = None
     if rank == 0 and (args.accuracy_steps > 0 or args.oracle_steps > 0):
         accuracy = accuracy_runs(w, args, torch)
+        nrb = accuracy.get("rebuilds_after_the_first", {}).get("mixed")
+        if nrb is not None and args.accuracy_steps > 1:
+            rebuild["rebuilds_in_accuracy_run"] = {"steps": args.accuracy_steps - 1, "rebuilds": nrb}
+            rebuild["amortised_ms_per_step"] = rebuild["rebuild_ms"] * nrb / (args.accuracy_steps - 1)
 
     # the learned capillary closure: samples of the plain formula logged from
     # the bed, trained by the library's own kernels, then the same bed stepped
@@ -839,14 +847,11 @@ def run_headline(args, ws, rank):
 
 
 def rebuild_cost(eng, n: int) -> dict:
-    """one forced rebuild of engine e timed kernel by kernel, and the rebuild
-    interval seen so far: the rebuild's share of a step, amortised"""
+    """one forced rebuild of engine e timed kernel by kernel (its share of a step
+    follows from the rebuild interval of a longer run: accuracy_runs)"""
     prof = eng.profile_kernels()
     ms = sum(t for name, t in prof if name != "step kernel")
-    st = eng.stats()
-    per = st["iter"] / max(1, st["rebuilds"])
-    return {"rebuild_ms": ms, "steps_per_rebuild_so_far": per, "amortised_ms_per_step": ms / per,
-            "kernels": {name: t for name, t in prof}}
+    return {"rebuild_ms": ms, "kernels": {name: t for name, t in prof}}
 
 
 def end_to_end(eng, n: int, steps: int, ws: int) -> tuple[float, dict]:
@@ -899,6 +904,7 @@ def accuracy_runs(w, args, torch) -> dict:
         e.step(args.accuracy_steps - short)
         e.sync()
         runs[name] = (e.get_state()["pos"], time.perf_counter() - t0)
+        out.setdefault("rebuilds_after_the_first", {})[name] = int(e.stats()["rebuilds"]) - 1
         e.close()
     if runs:
         mm, mr = packing_metrics(w.setup, runs["mixed"][0]), packing_metrics(w.setup, runs["fp64"][0])
