@@ -232,6 +232,83 @@ __global__ void k_export_gather(int n, const int* __restrict__ inv, const double
   if (i < n) dst[i] = src[inv[i]];
 }
 
+/* A caller's host array that kernels may read or write directly: page-locked
+ * (cudaHostAlloc, cudaMallocHost, cudaHostRegister) and mapped on the current
+ * device from its first byte to its last, with one contiguous device view;
+ * NULL otherwise, and the copy engines move it through device staging. */
+void* mapped_view(const void* p, size_t bytes) {
+  if (!p || bytes == 0) return nullptr;
+  cudaPointerAttributes a0, a1;
+  std::memset(&a0, 0, sizeof(a0));
+  std::memset(&a1, 0, sizeof(a1));
+  const char* last = static_cast<const char*>(p) + (bytes - 1);
+  if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return nullptr;
+  if (static_cast<const char*>(a1.devicePointer) - static_cast<const char*>(a0.devicePointer) != (ptrdiff_t)(bytes - 1))
+    return nullptr;
+  return a0.devicePointer;
+}
+
+/* The state import from mapped host arrays: thread i reads the caller's
+ * element i (a warp reads 768 contiguous bytes over the host link) and
+ * writes it at its cell position inv[i] */
+__global__ void k_import_mapped(int n, const int* __restrict__ inv, const double3* __restrict__ hp,
+                                const double3* __restrict__ hv, const double3* __restrict__ hw,
+                                double3* __restrict__ pos, double3* __restrict__ vel, double3* __restrict__ angv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int q = inv[i];
+  pos[q] = hp[i];
+  vel[q] = hv ? hv[i] : make_double3(0.0, 0.0, 0.0);
+  angv[q] = hw ? hw[i] : make_double3(0.0, 0.0, 0.0);
+}
+
+/* The state export into mapped host arrays in caller order (array k =
+ * blockIdx.y).  An array of n double3 is 3n doubles; thread t writes doubles
+ * 2t and 2t + 1 -- component c of particle i is double 3i + c, read from cell
+ * position inv[i] -- as one 16-byte store, so a warp writes 512 contiguous
+ * bytes over the host link (three 8-byte stores 24 bytes apart per particle
+ * leave partial lines: a third of the link's rate, measured).  A destination
+ * that is not 16-byte aligned takes 8-byte stores. */
+struct ExportSet {
+  const void* src[5];
+  int kind[5]; /* 0: double3 array, 1: float4 array (x y z), 2: zeros */
+  double* dst[5];
+  int count;
+};
+__device__ __forceinline__ double export_value(const void* src, int kind, int q, int c) {
+  if (kind == 0) return static_cast<const double*>(src)[3LL * q + c];
+  if (kind == 1) return (double)static_cast<const float*>(src)[4LL * q + c];
+  return 0.0;
+}
+__global__ void k_export_mapped(int n, const int* __restrict__ inv, ExportSet x) {
+  const int k = blockIdx.y;
+  if (k >= x.count) return;
+  const void* src = x.src[k];
+  const int kind = x.kind[k];
+  double* __restrict__ dst = x.dst[k];
+  const long long m = 3LL * n;
+  const long long e = 2LL * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (e >= m) return;
+  const long long i0 = e / 3, i1 = (e + 1) / 3;
+  const double v0 = export_value(src, kind, inv[i0], (int)(e - 3 * i0));
+  if (e + 1 < m) {
+    const double v1 = export_value(src, kind, inv[i1], (int)(e + 1 - 3 * i1));
+    if ((reinterpret_cast<size_t>(dst) & 15) == 0) {
+      *reinterpret_cast<double2*>(dst + e) = make_double2(v0, v1);
+    } else {
+      dst[e] = v0;
+      dst[e + 1] = v1;
+    }
+  } else {
+    dst[e] = v0;
+  }
+}
+
 __global__ void k_check_finite(int n, const double3* __restrict__ pos, const double3* __restrict__ vel,
                                int* __restrict__ err) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -313,6 +390,9 @@ dem_status enqueue_rebuild(dem_ctx* c, cudaStream_t s, int parity) {
                                            b.nwall, b.wlist_old, b.nwall_old, b.wrec_old, b.wrec,
                                            reorder ? b.sorted_src : nullptr, reorder ? b.old_to_new : nullptr, n);
   mark(c, s, "k_carry");
+  /* the caller-order view of the new cell order, for the state import and export */
+  k_inverse<<<grid_for(n, 256), 256, 0, s>>>(n, b.id, b.inv);
+  mark(c, s, "k_inverse");
   return cuda_check(cudaGetLastError(), "rebuild launch");
 }
 
@@ -533,7 +613,7 @@ namespace {
  * its allocation list (kept next to it), plus 2 MiB of rounding per allocation */
 dem_memory memory_of(long long N, long long S, long long C, const dem_options* o) {
   dem_memory m;
-  m.per_particle = 3 * 24 + 2 * 8 + 5 * 4      /* pos vel angv, rad pmove, lqd lqd_old id plevel nidx */
+  m.per_particle = 3 * 24 + 2 * 8 + 6 * 4      /* pos vel angv, rad pmove, lqd lqd_old id inv plevel nidx */
                    + 3 * 24 + 8 + 3 * 4        /* tmp copies used while permuting */
                    + 2 * 24                    /* staging of the force and moment exports */
                    + 2 * 24 + 8                /* force mom rmom */
@@ -679,7 +759,7 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
 #define A(ptr, count) \
   if (st == DEM_OK) st = dalloc(c, &(ptr), (count))
   A(b.pos, N); A(b.vel, N); A(b.angv, N); A(b.rad, N); A(b.pmove, N); A(b.lqd, N); A(b.lqd_old, N);
-  A(b.id, N); A(b.plevel, N); A(b.nidx, N);
+  A(b.id, N); A(b.inv, N); A(b.plevel, N); A(b.nidx, N);
   A(b.tmp_pos, N); A(b.tmp_vel, N); A(b.tmp_angv, N); A(b.tmp_rad, N); A(b.tmp_lqd, N); A(b.tmp_id, N);
   A(b.tmp_out, 2 * N);
   A(b.tmp_plevel, N);
@@ -718,6 +798,7 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
     std::vector<int> ids(N);
     for (size_t i = 0; i < N; i++) ids[i] = (int)i;
     up(b.id, ids.data(), sizeof(int) * N);
+    up(b.inv, ids.data(), sizeof(int) * N);
   }
   up(b.nidx, nebor_idx, sizeof(int) * N);
   const int one = 1;
@@ -836,15 +917,41 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
   if (!c || !pos) return fail(DEM_ERR_ARG, "dem_set_state: null argument");
   const size_t N = (size_t)c->n;
   EngineBufs& b = c->b;
-  /* host arrays (caller order) go to the tmp buffers (copy engine), then a
-   * gather by id into cell order */
   if (c->trace) cudaEventRecord(c->trace[0], c->stream);
+  /* page-locked caller arrays: one kernel reads them over the host link and
+   * writes the cell-ordered state (and, mixed, its shadows) directly */
+  const size_t bytes = sizeof(double3) * N;
+  const double3* mp = static_cast<const double3*>(mapped_view(pos, bytes));
+  const double3* mv = vel ? static_cast<const double3*>(mapped_view(vel, bytes)) : nullptr;
+  const double3* mw = angvel ? static_cast<const double3*>(mapped_view(angvel, bytes)) : nullptr;
+  if (mp && (!vel || mv) && (!angvel || mw)) {
+    if (!request_rebuild && c->opt.precision == DEM_PREC_MIXED) {
+      dem_status st = mixed_import_mapped(c, c->parity, b.inv, mp, mv, mw, c->stream);
+      if (st != DEM_OK) return st;
+    } else {
+      k_import_mapped<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.inv, mp, mv, mw, b.pos, b.vel, b.angv);
+    }
+    /* the event the host waits on comes last, so the trace's are done too */
+    cudaError_t e = cudaSuccess;
+    if (c->trace) e = cudaEventRecord(c->trace[1], c->stream);
+    if (e == cudaSuccess && c->trace) e = cudaEventRecord(c->trace[2], c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->xev[0], c->stream);
+    if (e == cudaSuccess && request_rebuild) {
+      const int one = 1;
+      e = cudaMemcpyAsync(b.need, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    }
+    if (e != cudaSuccess) return cuda_check(e, "dem_set_state import");
+    /* the caller's arrays are free again once the import has read them */
+    return cuda_check(cudaEventSynchronize(c->xev[0]), "dem_set_state");
+  }
+  /* other host arrays (caller order) go to the tmp buffers (copy engine),
+   * then a gather by id into cell order */
   cudaError_t e = cudaMemcpyAsync(b.tmp_pos, pos, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && vel) e = cudaMemcpyAsync(b.tmp_vel, vel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && angvel)
     e = cudaMemcpyAsync(b.tmp_angv, angvel, sizeof(double3) * N, cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) e = cudaEventRecord(c->xev[0], c->stream);
   if (e == cudaSuccess && c->trace) e = cudaEventRecord(c->trace[1], c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->xev[0], c->stream);
   if (e != cudaSuccess) return cuda_check(e, "dem_set_state upload");
   if (!request_rebuild && c->opt.precision == DEM_PREC_MIXED) {
     /* the neighbours read the shadow copy: the import refreshes it from the
@@ -873,7 +980,42 @@ extern "C" dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, doub
   EngineBufs& b = c->b;
   const size_t N = (size_t)c->n;
   if (c->trace) cudaEventRecord(c->trace[4], c->stream);
-  if (c->opt.precision == DEM_PREC_MIXED && (force || mom)) {
+  const bool mixed = c->opt.precision == DEM_PREC_MIXED;
+  /* page-locked caller arrays: one kernel gathers every requested array
+   * into caller order and writes it over the host link directly (mixed
+   * precision: the forces from the step's FP32 totals, no moments) */
+  {
+    const size_t bytes = sizeof(double3) * N;
+    double3* const host[5] = {pos, vel, angvel, force, mom};
+    double3* view[5] = {};
+    bool direct = pos || vel || angvel || force || mom;
+    for (int k = 0; k < 5 && direct; k++) {
+      if (!host[k]) continue;
+      view[k] = static_cast<double3*>(mapped_view(host[k], bytes));
+      direct = view[k] != nullptr;
+    }
+    if (direct) {
+      const void* const dev[5] = {b.pos, b.vel, b.angv, mixed ? (const void*)mixed_force_shadow(c) : b.force,
+                                  mixed ? nullptr : b.mom};
+      const int kind[5] = {0, 0, 0, mixed ? 1 : 0, mixed ? 2 : 0};
+      ExportSet x{};
+      for (int k = 0; k < 5; k++) {
+        if (!view[k]) continue;
+        x.src[x.count] = dev[k];
+        x.kind[x.count] = kind[k];
+        x.dst[x.count] = reinterpret_cast<double*>(view[k]);
+        x.count++;
+      }
+      const dim3 grid((unsigned)grid_for((3LL * c->n + 1) / 2, 256), (unsigned)x.count);
+      k_export_mapped<<<grid, 256, 0, c->stream>>>(c->n, b.inv, x);
+      cudaError_t e = cudaSuccess;
+      if (c->trace) e = cudaEventRecord(c->trace[5], c->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(c->xev[6], c->stream);
+      if (e != cudaSuccess) return cuda_check(e, "dem_get_state export");
+      return cuda_check(cudaEventSynchronize(c->xev[6]), "dem_get_state");
+    }
+  }
+  if (mixed && (force || mom)) {
     dem_status st = mixed_force_to_master(c, c->stream);
     if (st != DEM_OK) return st;
   }
@@ -887,20 +1029,19 @@ extern "C" dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, doub
    * array is gathered; the compute stream then waits for the copies (the
    * staging buffers are reused by the next import), the host for the last */
   double3* stage[5] = {b.tmp_pos, b.tmp_vel, b.tmp_angv, b.tmp_out, b.tmp_out + N};
-  k_inverse<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.id, b.tmp_id);
   int k = 0;
   cudaError_t e = cudaSuccess;
   for (auto& it : items) {
     if (!it.host || e != cudaSuccess) continue;
-    k_export_gather<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.tmp_id, it.dev, stage[k]);
+    k_export_gather<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, b.inv, it.dev, stage[k]);
     e = cudaEventRecord(c->xev[1 + k], c->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->xfer, c->xev[1 + k], 0);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(it.host, stage[k], sizeof(double3) * N, cudaMemcpyDeviceToHost, c->xfer);
     k++;
   }
-  if (e == cudaSuccess) e = cudaEventRecord(c->xev[6], c->xfer);
   if (e == cudaSuccess && c->trace) e = cudaEventRecord(c->trace[5], c->xfer);
+  if (e == cudaSuccess) e = cudaEventRecord(c->xev[6], c->xfer);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->xev[6], 0);
   if (e != cudaSuccess) return cuda_check(e, "dem_get_state");
   return cuda_check(cudaEventSynchronize(c->xev[6]), "dem_get_state");
@@ -1400,6 +1541,7 @@ extern "C" dem_status dem_load(dem_ctx* c, const char* path) {
   c->iter = hdr[0];
   c->ctime = ct;
   c->parity = 0;
+  k_inverse<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->b.id, c->b.inv);
   if (c->opt.precision == DEM_PREC_MIXED) st = mixed_shadows(c, 0, c->stream);
   if (st == DEM_OK) st = cuda_check(cudaStreamSynchronize(c->stream), "dem_load sync");
   return st;

@@ -44,6 +44,7 @@ struct EngineBufs {
   double3 *pos, *vel, *angv;
   double *rad, *pmove;
   int *lqd, *lqd_old, *id, *plevel, *nidx;
+  int* inv; /* inv[id[q]] = q: the cell position of each caller index, renewed at every rebuild */
   double3 *tmp_pos, *tmp_vel, *tmp_angv;
   double3* tmp_out; /* 2 N: staging of exported arrays beside the three above */
   double* tmp_rad;
@@ -147,6 +148,10 @@ dem_status mixed_step(dem_ctx* c, int which, cudaStream_t s);
  * tmp buffers, gathered into cell order with the shadow buffer `which`
  * rewritten, in one launch */
 dem_status mixed_import(dem_ctx* c, int which, int has_v, int has_w, cudaStream_t s);
+/* the same from mapped host arrays in caller order (hv, hw may be NULL: zero);
+ * inv[i] is caller index i's cell position */
+dem_status mixed_import_mapped(dem_ctx* c, int which, const int* inv, const double3* hp, const double3* hv,
+                               const double3* hw, cudaStream_t s);
 /* the mixed step's pair loop: one thread per particle (true) or warp-cooperative */
 bool mixed_thread_loop(const dem_ctx* c);
 /* the name of the step kernel mixed_step launches, e.g. "k_step_mixed<1,0>" */
@@ -155,6 +160,8 @@ const char* mixed_step_kernel_name(const dem_ctx* c);
 dem_status mixed_pre_rebuild(dem_ctx* c, int which, cudaStream_t s);
 /* download the last step's force totals into the FP64 force array */
 dem_status mixed_force_to_master(dem_ctx* c, cudaStream_t s);
+/* the last step's forces, FP32, cell order (x, y, z, unused) */
+const float4* mixed_force_shadow(const dem_ctx* c);
 
 /* chain.cu: the chaining kernel after a step (tail-launches the rebuild and
  * the next step), the countdown, and the reset of the rebuild request */

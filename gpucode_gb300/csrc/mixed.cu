@@ -1321,6 +1321,68 @@ __global__ void k_import_shadows(int n, const int* __restrict__ id, const double
   w4[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
 }
 
+/* the same import from mapped host arrays read in caller order: thread i
+ * reads the caller's element i over the host link and writes cell position
+ * inv[i] (state, bridge count and shadows) */
+constexpr int kImportThreads = 256;
+/* the block's slice of one mapped host array (kImportThreads particles,
+ * contiguous) into shared memory with 16-byte loads when it is 16-byte
+ * aligned (a slice of 256 double3 is 6144 bytes), else 8-byte loads */
+__device__ __forceinline__ void stage_slice(const double3* __restrict__ h, int n, double* sm) {
+  const long long i0 = (long long)blockIdx.x * kImportThreads;
+  const int cnt = (int)min((long long)kImportThreads, n - i0);
+  const double* src = reinterpret_cast<const double*>(h + i0);
+  const int nd = 3 * cnt;
+  if ((reinterpret_cast<size_t>(src) & 15) == 0) {
+    for (int t = threadIdx.x; 2 * t < nd; t += blockDim.x) {
+      if (2 * t + 1 < nd) {
+        const double2 v = *reinterpret_cast<const double2*>(src + 2 * t);
+        sm[2 * t] = v.x;
+        sm[2 * t + 1] = v.y;
+      } else {
+        sm[2 * t] = src[2 * t];
+      }
+    }
+  } else {
+    for (int t = threadIdx.x; t < nd; t += blockDim.x) sm[t] = src[t];
+  }
+}
+
+__global__ void __launch_bounds__(kImportThreads) k_import_shadows_mapped(
+    int n, const int* __restrict__ inv, const double3* __restrict__ hp, const double3* __restrict__ hv,
+    const double3* __restrict__ hw, double3* __restrict__ pos, double3* __restrict__ vel, double3* __restrict__ angv,
+    const double* __restrict__ rad, int* __restrict__ lqd, double3 off, int bin_exp, float lo_scale,
+    float4* __restrict__ phi, float4* __restrict__ plo, float4* __restrict__ v4, float4* __restrict__ w4) {
+  __shared__ double sp[3 * kImportThreads], sv[3 * kImportThreads], sw[3 * kImportThreads];
+  stage_slice(hp, n, sp);
+  if (hv) stage_slice(hv, n, sv);
+  if (hw) stage_slice(hw, n, sw);
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int t3 = 3 * threadIdx.x;
+  const int q = inv[i];
+  const double3 p = make_double3(sp[t3], sp[t3 + 1], sp[t3 + 2]);
+  const double3 v = hv ? make_double3(sv[t3], sv[t3 + 1], sv[t3 + 2]) : make_double3(0.0, 0.0, 0.0);
+  const double3 w = hw ? make_double3(sw[t3], sw[t3 + 1], sw[t3 + 2]) : make_double3(0.0, 0.0, 0.0);
+  pos[q] = p;
+  vel[q] = v;
+  angv[q] = w;
+  const int lq = __float_as_int(v4[q].w);
+  lqd[q] = lq;
+  float4 ph, pl;
+  split_hi_lo(p.x + off.x, bin_exp, lo_scale, ph.x, pl.x);
+  split_hi_lo(p.y + off.y, bin_exp, lo_scale, ph.y, pl.y);
+  split_hi_lo(p.z + off.z, bin_exp, lo_scale, ph.z, pl.z);
+  const double r = rad[q];
+  ph.w = (float)r;
+  pl.w = (float)(r - (double)ph.w);
+  phi[q] = ph;
+  plo[q] = pl;
+  v4[q] = make_float4(d2f(v.x), d2f(v.y), d2f(v.z), __int_as_float(lq));
+  w4[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
+}
+
 __global__ void k_force_out(int n, const float4* __restrict__ f, double3* __restrict__ force, double3* __restrict__ mom) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -1426,6 +1488,16 @@ dem_status mixed_import(dem_ctx* c, int which, int has_v, int has_w, cudaStream_
   return cuda_check(cudaGetLastError(), "mixed_import launch");
 }
 
+dem_status mixed_import_mapped(dem_ctx* c, int which, const int* inv, const double3* hp, const double3* hv,
+                               const double3* hw, cudaStream_t s) {
+  MixedState* m = c->mx;
+  EngineBufs& b = c->b;
+  k_import_shadows_mapped<<<grid_for(c->n, kImportThreads), kImportThreads, 0, s>>>(c->n, inv, hp, hv, hw, b.pos, b.vel, b.angv, b.rad,
+                                                               b.lqd, m->off, m->bin_exp, m->lo_scale, m->phi[which],
+                                                               m->plo[which], m->vel[which], m->angv[which]);
+  return cuda_check(cudaGetLastError(), "mixed_import_mapped launch");
+}
+
 Prefilter mixed_prefilter(dem_ctx* c, int which) {
   /* |(hi_i - hi_j) - (x_i - x_j)| <= one binade ulp per axis (the lo parts are
    * below half an ulp each): sqrt(3) ulps, plus FP32 rounding of the distance
@@ -1520,6 +1592,8 @@ dem_status mixed_pre_rebuild(dem_ctx* c, int which, cudaStream_t s) {
   k_lqd_from_shadow<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, c->mx->vel[which], c->b.lqd);
   return cuda_check(cudaGetLastError(), "mixed_pre_rebuild launch");
 }
+
+const float4* mixed_force_shadow(const dem_ctx* c) { return c->mx ? c->mx->force : nullptr; }
 
 dem_status mixed_force_to_master(dem_ctx* c, cudaStream_t s) {
   k_force_out<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, c->mx->force, c->b.force, c->b.mom);

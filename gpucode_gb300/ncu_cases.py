@@ -4,9 +4,11 @@ Every kernel launch of these cases comes from the host (no CUDA graphs, no
 device-launched steps), so a profiler's launch counting (-s / -c) addresses
 them directly, and each case holds a few GB on the device at most.
 
-    python -m gpucode_gb300.ncu_cases step [--pairs thread|warp] [--steps 4]
+    python -m gpucode_gb300.ncu_cases step [--pairs thread|warp] [--steps 4] [--io]
         the packed 200,000-sphere wet bed: `steps` host-launched mixed steps
-        (the first rebuilds the lists); one step kernel per step
+        (the first rebuilds the lists); one step kernel per step; with --io
+        then an export, an import and one more step through page-locked host
+        arrays
     python -m gpucode_gb300.ncu_cases closure [--rows 1000000]
         the packed bed with the per-contact liquid model: a network trained
         for 3 epochs on the bridges of one step, 3 host-launched steps with it
@@ -24,7 +26,7 @@ BED = ROOT / "tests" / "golden" / "packed_wet200k.npz"
 LIQUID = {"vol_min": 0.005, "vol_max": 0.02, "theta_max": 0.5235987755982988, "seed": 2}
 
 
-def step_case(pairs: str, steps: int) -> None:
+def step_case(pairs: str, steps: int, io: bool = False) -> None:
     from . import configs
     from .engine import Engine
 
@@ -33,6 +35,19 @@ def step_case(pairs: str, steps: int) -> None:
     e.set_state(w.pos0_reduced)
     e.step(steps)
     e.sync()
+    if io:
+        # one end-to-end round trip through page-locked host arrays: the
+        # state import and export kernels that read and write them directly
+        import torch
+
+        from ._abi import check, ptr
+
+        n = w.setup.n
+        h = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+        check(e.lib.dem_get_state(e.h, ptr(h[0]), ptr(h[1]), ptr(h[2]), None, None), "dem_get_state")
+        check(e.lib.dem_set_state_ex(e.h, ptr(h[0]), ptr(h[1]), ptr(h[2]), 0), "dem_set_state_ex")
+        e.step(1)
+        check(e.lib.dem_get_state(e.h, ptr(h[0]), ptr(h[1]), ptr(h[2]), ptr(h[3]), None), "dem_get_state")
     print("ok", e.step_kernel_name(), e.stats())
     e.close()
 
@@ -77,9 +92,10 @@ def main(argv=None) -> None:
     ap.add_argument("--pairs", default="auto", choices=["auto", "warp", "thread"])
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--rows", type=int, default=1_000_000)
+    ap.add_argument("--io", action="store_true", help="step: then a round trip through page-locked host arrays")
     a = ap.parse_args(argv)
     if a.case == "step":
-        step_case(a.pairs, a.steps)
+        step_case(a.pairs, a.steps, a.io)
     else:
         closure_case(a.rows)
 

@@ -310,8 +310,11 @@ dem_status dem_create(const dem_setup* s, const double* rad, const int* plevel,
 dem_status dem_destroy(dem_ctx* c);
 /* Host state in the reference's double3 layout and particle order (reduced
  * units).  vel/angvel may be NULL (zero).  Marks the lists for rebuild.
- * Returns once the caller's arrays have been read; the device work behind
- * the copies stays queued on the context's stream. */
+ * Returns once the caller's arrays have been read.  Page-locked arrays
+ * (cudaHostAlloc, cudaMallocHost, cudaHostRegister, a framework's pinned
+ * buffers) are read by the import kernel itself over the host link, with no
+ * staging copy; pageable arrays go through the copy engines, and the device
+ * work behind those copies stays queued on the context's stream. */
 dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel);
 /* As dem_set_state, but with request_rebuild = 0 the current neighbour lists,
  * contact history and path-length accumulators are kept: for callers that
@@ -320,7 +323,10 @@ dem_status dem_set_state(dem_ctx* c, const double3* pos, const double3* vel, con
 dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel,
                             int request_rebuild);
 /* Any pointer may be NULL.  force/mom are the last step's totals.  Returns
- * when every requested array is written. */
+ * when every requested array is written.  When every requested array is
+ * page-locked one kernel gathers them into caller order and writes them over
+ * the host link directly; otherwise each goes through device staging and the
+ * copy engines. */
 dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,
                          double3* mom);
 /* Advance nsteps time steps.  Device-resident; no host synchronisation inside
@@ -377,9 +383,11 @@ const char* dem_step_kernel(dem_ctx* c);
  * dem_step(1) -> dem_get_state(pos, vel, angvel, force) on pinned or pageable
  * host arrays, with timing events at the calls' boundaries.  out[9], each the
  * mean in ms: [0] host wall time of the sequence; device spans [1] upload
- * copies, [2] import and shadows (plus the host's return), [3] from the
- * import to the end of the step (the host's launch of the step included),
- * [4] from the step to the export's start, [5] export gathers and copies;
+ * copies (page-locked arrays: the import kernel that reads them), [2] import
+ * and shadows (plus the host's return; ~0 for page-locked arrays), [3] from
+ * the import to the end of the step (the host's launch of the step included),
+ * [4] from the step to the export's start, [5] export gathers and copies
+ * (page-locked arrays: the one export kernel);
  * host time inside [6] dem_set_state_ex, [7] dem_step, [8] dem_get_state.
  * The state goes round trip unchanged but for the steps taken. */
 dem_status dem_e2e_parts(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force, int reps,

@@ -16,11 +16,11 @@ def test_estimate_adds_up():
     s = w.setup.s
     m = w.setup.memory("mixed")
     assert m["slots"] == s.n_pp_slots
-    assert m["per_slot"] == 138 and m["per_particle"] == 752 + 144
+    assert m["per_slot"] == 138 and m["per_particle"] == 756 + 144
     assert m["per_cell"] == 12  # cell start, end and offset
     low = m["per_particle"] * s.np + m["per_slot"] * s.n_pp_slots + m["per_cell"] * s.sys_ncells
     assert low < m["total"] < low + 200 * 2 ** 20
-    assert w.setup.memory("fp64")["per_particle"] == 752
+    assert w.setup.memory("fp64")["per_particle"] == 756
 
 
 def test_fit_memory_scales_slots_to_the_budget():
