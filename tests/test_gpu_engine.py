@@ -239,8 +239,9 @@ def test_state_round_trip_without_rebuild_is_bit_exact(cuda, precision):
 @pytest.mark.parametrize("rebuild", [0, 1])
 def test_page_locked_host_arrays_give_the_same_state(cuda, precision, rebuild):
     """Page-locked caller arrays are read and written by the import and export
-    kernels directly over the host link (no staging copy); pageable ones go
-    through the copy engines and device staging.  Both routes move the same
+    kernels directly over the host link (no staging copy; 16-byte accesses, or
+    8-byte ones for arrays that are not 16-byte aligned); pageable ones go
+    through the copy engines and device staging.  All routes move the same
     bits: three rounds of import, 7 steps and export (positions, velocities,
     spins and forces) give identical states and rebuild counts."""
     torch = pytest.importorskip("torch")
@@ -248,17 +249,22 @@ def test_page_locked_host_arrays_give_the_same_state(cuda, precision, rebuild):
     pos, vel, ang = _workloads.stirred(w)
     n = w.setup.n
     pinned = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+    # page-locked arrays that start 8 bytes into their allocation: the import
+    # and export take their 8-byte (not 16-byte) host accesses
+    odd = [torch.empty(3 * n + 1, dtype=torch.float64, pin_memory=True).numpy()[1:].reshape(n, 3) for _ in range(4)]
+    assert all(a.ctypes.data % 16 == 8 for a in odd)
     out = {}
-    for route in ("pageable", "page-locked"):
+    for route in ("pageable", "page-locked", "page-locked, 8-byte aligned"):
         e = Engine(w.setup, precision=precision)
         e.set_state(pos, vel, ang)
         e.step(20)
         st = e.get_state()
         bufs = [np.ascontiguousarray(st[k]) for k in ("pos", "vel", "angvel")] + [np.zeros((n, 3))]
-        if route == "page-locked":
-            for dst, src in zip(pinned, bufs):
+        if route != "pageable":
+            locked = pinned if route == "page-locked" else odd
+            for dst, src in zip(locked, bufs):
                 dst[...] = src
-            bufs = pinned
+            bufs = locked
         p, v, g, f = bufs
         for _ in range(3):
             _abi.check(e.lib.dem_set_state_ex(e.h, _abi.ptr(p), _abi.ptr(v), _abi.ptr(g), rebuild), "set_state_ex")
@@ -267,9 +273,10 @@ def test_page_locked_host_arrays_give_the_same_state(cuda, precision, rebuild):
                        "get_state")
         out[route] = ([b.copy() for b in (p, v, g, f)], e.stats()["rebuilds"])
         e.close()
-    for k, (a, b) in enumerate(zip(out["pageable"][0], out["page-locked"][0])):
-        assert np.array_equal(a, b), ("pos", "vel", "angvel", "force")[k]
-    assert out["pageable"][1] == out["page-locked"][1]
+    for route in ("page-locked", "page-locked, 8-byte aligned"):
+        for k, (a, b) in enumerate(zip(out["pageable"][0], out[route][0])):
+            assert np.array_equal(a, b), (route, ("pos", "vel", "angvel", "force")[k])
+        assert out["pageable"][1] == out[route][1], route
 
 
 def test_slot_overflow_is_reported_not_written(cuda):
