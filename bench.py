@@ -855,9 +855,11 @@ def rebuild_cost(eng, n: int) -> dict:
 
 
 def end_to_end(eng, n: int, steps: int, ws: int) -> tuple[float, dict]:
-    """particle-steps/s through dem_set_state_ex + dem_step + dem_get_state with
-    pinned host buffers (state in, one step, state and force out), and where
-    the time of such a step goes (dem_e2e_parts)"""
+    """particle-steps/s through the public C-ABI with pinned host buffers, one
+    step per round trip (state in, one step, state and force out): dem_advance,
+    which queues the import, the step and the export and waits once; the same
+    through the three calls dem_set_state_ex + dem_step + dem_get_state; and
+    where the time of the three-call step goes (dem_e2e_parts)"""
     import ctypes as C
 
     import torch
@@ -872,16 +874,24 @@ def end_to_end(eng, n: int, steps: int, ws: int) -> tuple[float, dict]:
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
+        check(eng.lib.dem_advance(eng.h, ptr(hp), ptr(hv), ptr(hw), ptr(hf), 1), "dem_advance")
+    e2e_t = time.perf_counter() - t0
+    rate, _ = replica_rate(e2e_t, n, steps, ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
         check(eng.lib.dem_set_state_ex(eng.h, ptr(hp), ptr(hv), ptr(hw), 0), "dem_set_state_ex")
         check(eng.lib.dem_step(eng.h, 1), "dem_step")
         check(eng.lib.dem_get_state(eng.h, ptr(hp), ptr(hv), ptr(hw), ptr(hf), None), "dem_get_state")
-    e2e_t = time.perf_counter() - t0
-    rate, _ = replica_rate(e2e_t, n, steps, ws)
+    three_t = time.perf_counter() - t0
     out = (C.c_double * 9)()
     check(eng.lib.dem_e2e_parts(eng.h, ptr(hp), ptr(hv), ptr(hw), ptr(hf), 10, out), "dem_e2e_parts")
     names = ["host_total", "dev_upload_copies", "dev_import_shadows", "dev_to_step_end", "dev_step_to_export",
              "dev_export_gather_copies", "host_in_set_state", "host_in_step", "host_in_get_state"]
-    return rate, {k: out[i] for i, k in enumerate(names)}
+    parts = {k: out[i] for i, k in enumerate(names)}
+    parts["ms_per_step_dem_advance"] = 1000.0 * e2e_t / steps
+    parts["ms_per_step_three_calls"] = 1000.0 * three_t / steps
+    return rate, parts
 
 
 def accuracy_runs(w, args, torch) -> dict:

@@ -230,6 +230,7 @@ def _declare(lib: C.CDLL) -> None:
         "dem_destroy": (I, [P]),
         "dem_set_state": (I, [P, P, P, P]),
         "dem_set_state_ex": (I, [P, P, P, P, I]),
+        "dem_advance": (I, [P, P, P, P, P, I]),
         "dem_profile_step": (I, [P, I, P, C.c_size_t, C.POINTER(C.c_double)]),
         "dem_get_state": (I, [P, P, P, P, P, P]),
         "dem_step": (I, [P, I]),

@@ -912,8 +912,12 @@ extern "C" dem_status dem_set_state(dem_ctx* c, const double3* pos, const double
   return dem_set_state_ex(c, pos, vel, angvel, 1);
 }
 
-extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel,
-                                       int request_rebuild) {
+namespace {
+/* The state import (dem_set_state_ex).  wait: return once the caller's arrays
+ * have been read; otherwise return with the reads queued on the context's
+ * stream (dem_advance, which waits at its end). */
+dem_status state_import(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel,
+                        int request_rebuild, bool wait) {
   if (!c || !pos) return fail(DEM_ERR_ARG, "dem_set_state: null argument");
   const size_t N = (size_t)c->n;
   EngineBufs& b = c->b;
@@ -942,7 +946,7 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
     }
     if (e != cudaSuccess) return cuda_check(e, "dem_set_state import");
     /* the caller's arrays are free again once the import has read them */
-    return cuda_check(cudaEventSynchronize(c->xev[0]), "dem_set_state");
+    return wait ? cuda_check(cudaEventSynchronize(c->xev[0]), "dem_set_state") : DEM_OK;
   }
   /* other host arrays (caller order) go to the tmp buffers (copy engine),
    * then a gather by id into cell order */
@@ -970,8 +974,26 @@ extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const dou
   if (c->trace) cudaEventRecord(c->trace[2], c->stream);
   /* the caller's arrays are free again once the copies are done; the import
    * and the shadows run on behind them, ahead of the next step */
+  if (!wait) return DEM_OK;
   e = cudaEventSynchronize(c->xev[0]);
   return cuda_check(e, "dem_set_state");
+}
+}  // namespace
+
+extern "C" dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const double3* vel, const double3* angvel,
+                                       int request_rebuild) {
+  return state_import(c, pos, vel, angvel, request_rebuild, true);
+}
+
+extern "C" dem_status dem_advance(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,
+                                  int nsteps) {
+  if (!c || !pos || nsteps < 0) return fail(DEM_ERR_ARG, "dem_advance: bad argument");
+  /* import, steps and export queued back to back on the context's stream;
+   * the host waits once, for the export */
+  dem_status st = state_import(c, pos, vel, angvel, 0, false);
+  if (st == DEM_OK) st = dem_step(c, nsteps);
+  if (st == DEM_OK) st = dem_get_state(c, pos, vel, angvel, force, nullptr);
+  return st;
 }
 
 extern "C" dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,

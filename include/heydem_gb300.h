@@ -329,6 +329,16 @@ dem_status dem_set_state_ex(dem_ctx* c, const double3* pos, const double3* vel, 
  * copy engines. */
 dem_status dem_get_state(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force,
                          double3* mom);
+/* One round trip for a caller that keeps the state in host memory: import
+ * pos/vel/angvel (as dem_set_state_ex with request_rebuild = 0; vel/angvel may
+ * be NULL: zero, and then not exported), advance nsteps, export
+ * pos/vel/angvel/force back into the same arrays (force may be NULL).  The
+ * three are queued back to back and the host waits once, at the end, so the
+ * device does not idle while the host returns from the import and launches
+ * the steps.  Page-locked arrays are read and written directly (as in
+ * dem_set_state_ex / dem_get_state).  The caller's arrays must not be touched
+ * until it returns. */
+dem_status dem_advance(dem_ctx* c, double3* pos, double3* vel, double3* angvel, double3* force, int nsteps);
 /* Advance nsteps time steps.  Device-resident; no host synchronisation inside
  * unless the context was created without graphs. */
 dem_status dem_step(dem_ctx* c, int nsteps);

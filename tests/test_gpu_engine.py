@@ -279,6 +279,43 @@ def test_page_locked_host_arrays_give_the_same_state(cuda, precision, rebuild):
         assert out["pageable"][1] == out[route][1], route
 
 
+@pytest.mark.parametrize("locked", [False, True])
+def test_advance_equals_import_step_export(cuda, locked):
+    """dem_advance (import, steps and export with one wait) against the three
+    calls it queues, on page-locked and on pageable arrays: the same bits in
+    the same arrays, four rounds of 9 steps"""
+    torch = pytest.importorskip("torch")
+    w = _workloads.small_wet()
+    pos, vel, ang = _workloads.stirred(w)
+    n = w.setup.n
+    out = {}
+    for call in ("three calls", "dem_advance"):
+        e = Engine(w.setup, precision="mixed")
+        e.set_state(pos, vel, ang)
+        e.step(30)
+        st = e.get_state()
+        if locked:
+            bufs = [torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+        else:
+            bufs = [np.empty((n, 3)) for _ in range(4)]
+        for dst, k in zip(bufs, ("pos", "vel", "angvel", "force")):
+            dst[...] = st[k]
+        p, v, g, f = bufs
+        for _ in range(4):
+            if call == "dem_advance":
+                _abi.check(e.lib.dem_advance(e.h, _abi.ptr(p), _abi.ptr(v), _abi.ptr(g), _abi.ptr(f), 9), "advance")
+            else:
+                _abi.check(e.lib.dem_set_state_ex(e.h, _abi.ptr(p), _abi.ptr(v), _abi.ptr(g), 0), "set_state_ex")
+                e.step(9)
+                _abi.check(e.lib.dem_get_state(e.h, _abi.ptr(p), _abi.ptr(v), _abi.ptr(g), _abi.ptr(f), None), "get")
+        out[call] = ([b.copy() for b in bufs], e.stats()["rebuilds"], e.stats()["iter"])
+        e.close()
+    a, b = out["three calls"], out["dem_advance"]
+    for k in range(4):
+        assert np.array_equal(a[0][k], b[0][k]), ("pos", "vel", "angvel", "force")[k]
+    assert a[1:] == b[1:]
+
+
 def test_slot_overflow_is_reported_not_written(cuda):
     """A level whose slot capacity is too small: the build stops at capacity and
     dem_sync reports DEM_ERR_OVERFLOW (the reference would write past the end)."""
