@@ -316,23 +316,27 @@ __device__ __forceinline__ float bridge_rupture32(const MixArgs& a, float V, flo
   return a.lq_mode ? rupture32(V, th) : 0.99f * exp2f(0.33f * __log2f(V));
 }
 
+/* A contact record is read once and written once per step: streaming
+ * (evict-first) loads and stores keep it from displacing the partners'
+ * shadows, which a warp's neighbours read again, from L1 (114.6 vs 118.5 us
+ * on the packed 200k bed, the same bits) */
 __device__ __forceinline__ MixedRec load_rec(const ContactRec* p) {
   const float4* q = reinterpret_cast<const float4*>(p);
   MixedRec r;
   float4* o = reinterpret_cast<float4*>(&r);
-  o[0] = q[0];
-  o[1] = q[1];
-  o[2] = q[2];
-  o[3] = q[3];
+  o[0] = __ldcs(q + 0);
+  o[1] = __ldcs(q + 1);
+  o[2] = __ldcs(q + 2);
+  o[3] = __ldcs(q + 3);
   return r;
 }
 __device__ __forceinline__ void store_rec(ContactRec* p, const MixedRec& r) {
   float4* q = reinterpret_cast<float4*>(p);
   const float4* o = reinterpret_cast<const float4*>(&r);
-  q[0] = o[0];
-  q[1] = o[1];
-  q[2] = o[2];
-  q[3] = o[3];
+  __stcs(q + 0, o[0]);
+  __stcs(q + 1, o[1]);
+  __stcs(q + 2, o[2]);
+  __stcs(q + 3, o[3]);
 }
 
 /* One p-p contact (gap < 0, unit vector u from j to i): relative velocity at
