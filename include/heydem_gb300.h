@@ -280,7 +280,7 @@ typedef struct dem_options {
   int precision;          /* DEM_PREC_* */
   int capillary;          /* DEM_CAP_* */
   int block_size;         /* threads per block of the step kernel, a multiple of 32 up to 128
-                             (0 = default: 32 for the WARP loop, 64 for THREAD, 128 with the
+                             (0 = default: 32 for the WARP loop, 128 for THREAD and with the
                              learned closure) */
   int reorder;            /* 1: keep particles in cell order (default); 0: reference order */
   int use_graph;          /* 1: replay steps through a CUDA graph (default) */

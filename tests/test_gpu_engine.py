@@ -114,7 +114,7 @@ def test_pair_loops_agree(cuda, make):
 
 @pytest.mark.parametrize("pairs, sizes", [("warp", (32, 64, 96, 128)), ("thread", (32, 64, 128))])
 def test_block_size_does_not_change_results(cuda, pairs, sizes):
-    """The step kernel's block size (the default, 32 for the warp loop and 64
+    """The step kernel's block size (the default, 32 for the warp loop and 128
     for the thread loop, or the option) only changes which warps share a
     block: every warp's particles and arithmetic are the same, so 60 steps
     with rebuilds give the same bits at every size."""
