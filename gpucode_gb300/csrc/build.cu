@@ -43,18 +43,7 @@ __global__ void k_hash_count(const double3* __restrict__ pos, const int* __restr
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int lvl = plevel[i];
-  /* grid_pos's cell, with the unclamped indices kept: a particle beyond a
-   * face of its grid, which the clamp puts into a cell that does not contain
-   * it, sets *lv.outside (the neighbour search then walks whole windows) */
-  const double3 p = pos[i];
-  const double cs = lv.cell_size[lvl];
-  const int3 gs = lv.grid_size[lvl];
-  const int ux = (int)floor((p.x - origin.x) / cs), uy = (int)floor((p.y - origin.y) / cs),
-            uz = (int)floor((p.z - origin.z) / cs);
-  if (lv.outside && !(ux >= 0 && uy >= 0 && uz >= 0 && ux < gs.x && uy < gs.y && uz < gs.z))
-    atomicOr(lv.outside, 1);
-  const int3 gc = make_int3(max(0, min(ux, gs.x)), max(0, min(uy, gs.y)), max(0, min(uz, gs.z)));
-  int h = grid_hash(gc, lvl, lv);
+  int h = grid_hash(grid_pos(pos[i], lvl, lv, origin), lvl, lv);
   if (lvl != 0) h += lv.ncell_idx[lvl - 1];
   /* the reference clamps to gridSize (not gridSize-1, kernel.cu:627-629), so a
    * particle on the far face of the last level's grid hashes past the end; it
@@ -259,34 +248,7 @@ __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* _
     if (cell_off) {
       /* rows r = (z + off) W + (y + off), in the reference's (z, y) order;
        * the ranges of kRowBatch rows are read with independent loads before
-       * their particles are visited in order.
-       *
-       * With the level's largest radius known, a row's cells that lie wholly
-       * beyond the largest cut-off this particle can have against that level
-       * (r_i + r_max + skin, plus a margin above the FP32 prefilter's and the
-       * cell assignment's rounding) are skipped: they hold no neighbour, so
-       * the list is the same, entry for entry.  The window the reference
-       * walks, (2 ceil(size_L / size_l) + 1)^3 cells, is far larger than that
-       * sphere for a large particle searching a small level.  Only while every
-       * particle lies inside its grid (*outside == 0): the reference's clamp
-       * puts a particle beyond a face into a cell that does not contain it. */
-      const double* rmx = (lv.level_rmax && lv.outside && *lv.outside == 0) ? lv.level_rmax : nullptr;
-      /* the skipping's geometry in FP32 (FP64 divides and square roots are
-       * slow here), relative to the grid's origin, with a margin of 1e-5 of
-       * the coordinates' scale: far above FP32 rounding, far below a cell */
-      float R2 = -1.f; /* squared cut-off radius of the skipping, < 0: off */
-      float csf = 0.f, inv_cs = 0.f, px = 0.f, py = 0.f, pz = 0.f;
-      if (rmx) {
-        const double cs = lv.cell_size[iL];
-        csf = (float)cs;
-        inv_cs = (float)(1.0 / cs);
-        px = (float)(o.x - origin.x);
-        py = (float)(o.y - origin.y);
-        pz = (float)(o.z - origin.z);
-        const float reach = (float)(ri + rmx[iL] + search_gap);
-        const float margin = 2.0f * pre.tol + 1e-5f * (1.0f + fabsf(px) + fabsf(py) + fabsf(pz) + reach);
-        R2 = (reach + margin) * (reach + margin);
-      }
+       * their particles are visited in order */
       const int W = 2 * off + 1, R = W * W;
       for (int r0 = 0; r0 < R; r0 += kRowBatch) {
         int rf[kRowBatch], rl[kRowBatch];
@@ -301,24 +263,8 @@ __global__ void k_neighbor_find(const double3* __restrict__ pos, const double* _
           if (e.x > gs.x - 1) e.x = gs.x - 1;
           if (r < R && !(s.y < 0 || s.z < 0 || s.y > gs.y - 1 || s.z > gs.z - 1) && e.x >= s.x) {
             const int row = grid_hash(s, iL, lv) + cell_sum;
-            int xa = s.x, xb = e.x; /* the cells of the row to walk */
-            if (R2 >= 0.f) {
-              const float ylo = s.y * csf, zlo = s.z * csf;
-              const float dy = fmaxf(0.f, fmaxf(ylo - py, py - (ylo + csf)));
-              const float dz = fmaxf(0.f, fmaxf(zlo - pz, pz - (zlo + csf)));
-              const float rest = R2 - (dy * dy + dz * dz);
-              if (rest <= 0.f) {
-                xa = e.x + 1;
-              } else {
-                const float hw = sqrtf(rest);
-                xa = max(xa, (int)floorf((px - hw) * inv_cs));
-                xb = min(xb, (int)floorf((px + hw) * inv_cs));
-              }
-            }
-            if (xa <= xb) {
-              rf[b] = __ldg(cell_off + row + (xa - s.x));
-              rl[b] = __ldg(cell_off + row + (xb - s.x) + 1);
-            }
+            rf[b] = __ldg(cell_off + row);
+            rl[b] = __ldg(cell_off + row + (e.x - s.x) + 1);
           }
         }
 #pragma unroll
@@ -484,7 +430,6 @@ dem_status cell_sort(const double3* pos, const int* plevel, const int* order_key
   int* tile = rank + n;
   const int ntiles = div_up(ncells, kScanTile);
   cudaError_t e = cudaMemsetAsync(cell_end, 0, sizeof(int) * (size_t)ncells, stream);
-  if (e == cudaSuccess && lv.outside) e = cudaMemsetAsync(lv.outside, 0, sizeof(int), stream);
   if (e != cudaSuccess) return cuda_check(e, "cell_sort memset");
   if (n > 0)
     k_hash_count<<<grid_for(n, 256), 256, 0, stream>>>(pos, plevel, n, lv, k.prm.Origin, ncells, key, rank,

@@ -53,12 +53,6 @@ struct LevelView {
   const int* level_npars;
   const int* level_nnebors;
   int n_levels;
-  /* per level the largest particle radius (reduced), and a word the cell
-   * sort sets when a particle lies beyond a face of its grid; with both, the
-   * neighbour search skips the window's cells beyond the largest cut-off.
-   * NULL: it walks every cell of the reference's window */
-  const double* level_rmax = nullptr;
-  int* outside = nullptr;
 };
 
 /* contact history, reference layout (heydem.h:153-190, the fields in use) */

@@ -770,7 +770,6 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   A(b.sorted_hash, N); A(b.sorted_src, N); A(b.old_to_new, N); A(b.cell_start, C); A(b.cell_end, C);
   A(b.cell_off, C + 1);
   A(b.cell_size, L); A(b.grid_size, L); A(b.ncell_idx, L); A(b.npars, L); A(b.nneb, L); A(b.level_size, L);
-  A(b.level_rmax, L); A(b.outside, 1);
   A(b.cyl, 1); A(b.flag, 1); A(b.need, 1); A(b.err, 1); A(b.counters, 8);
 #undef A
   if (st == DEM_OK) {
@@ -795,12 +794,6 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   up(b.cyl, &s->cyl, sizeof(CylinderBC));
   up(b.rad, rad, sizeof(double) * N);
   up(b.plevel, plevel, sizeof(int) * N);
-  {
-    std::vector<double> rmax(L, 0.0);
-    for (size_t i = 0; i < N; i++)
-      if (plevel[i] >= 0 && plevel[i] < L) rmax[plevel[i]] = std::max(rmax[plevel[i]], rad[i]);
-    up(b.level_rmax, rmax.data(), sizeof(double) * L);
-  }
   if (st == DEM_OK) {
     std::vector<int> ids(N);
     for (size_t i = 0; i < N; i++) ids[i] = (int)i;
@@ -817,8 +810,6 @@ extern "C" dem_status dem_create(const dem_setup* s, const double* rad, const in
   c->lv.level_npars = b.npars;
   c->lv.level_nnebors = b.nneb;
   c->lv.n_levels = s->n_levels;
-  c->lv.level_rmax = b.level_rmax;
-  c->lv.outside = b.outside;
   if (st == DEM_OK && c->opt.precision == DEM_PREC_MIXED) st = mixed_create(c);
   if (st != DEM_OK) {
     dem_destroy(c);

@@ -66,8 +66,6 @@ struct EngineBufs {
   int3* grid_size;
   int *ncell_idx, *npars, *nneb;
   double* level_size;
-  double* level_rmax; /* per level the largest radius (the neighbour search's cell skipping) */
-  int* outside;       /* set by the cell sort: a particle beyond a face of its grid */
   CylinderBC* cyl; /* one cylinder, or one per system when systems are batched */
   /* batched systems (NULL for one system): system of each particle id, and
    * whether each system is wet */
