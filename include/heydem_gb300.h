@@ -270,10 +270,11 @@ enum { DEM_PREC_FP64 = 0, DEM_PREC_MIXED = 1 };
 enum { DEM_CAP_FORMULA = 0, DEM_CAP_MLP = 1 };
 /* pair loop of the mixed step kernel: the warp's lanes share out its particles'
  * pairs (WARP), or one thread walks one particle's pairs (THREAD); AUTO (the
- * default) takes THREAD, the faster of the two on a packed bed (6.4 contacts
- * per sphere: 122 vs 155 us on the packed 200k wet bed).  WARP is faster on
- * loose beds, where most lanes of a thread loop idle (68 vs 74 us on a
- * sequentially deposited 200k bed with 2.2 contacts per sphere). */
+ * default) takes THREAD, the faster of the two on packed and loose beds alike
+ * (114.6 vs 157.2 us on the packed 200k wet bed, 6.4 contacts per sphere;
+ * 505 vs 634 us on a sequentially deposited 2M bed, 2.2 contacts per sphere).
+ * WARP, the same formulas in phases over the warp's compacted pairs, stays
+ * selectable and tested. */
 enum { DEM_PAIRS_AUTO = 0, DEM_PAIRS_WARP = 1, DEM_PAIRS_THREAD = 2 };
 
 typedef struct dem_options {
