@@ -134,7 +134,7 @@ struct LawCfg64 {
   double rot_eps;  /* 1e-7 (p-p) / 1e-10 (wall): spring rotation guard */
   double dsmx_eps; /* 1e-7 (p-p) / 1e-10 (wall): slip-ratio and rescale guard */
   bool damp_on;    /* p-p: stage == 1; wall: stage == 1 || 7 */
-  double dmp_sq;   /* dmpn product under the damping sqrt */
+  double dmp;      /* sqrt of the dmpn product (the reference takes it per contact) */
 };
 
 /* elasto-plastic Hertz normal force + damping + tangential spring with slip
@@ -143,6 +143,8 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
                                               double3 cpv, HistRec& h, double iRad, double rfrc,
                                               double dt, double3& dF, double3& dM, double& dR) {
   const calParaPP& cal = *c.cal;
+  /* pow(ijRad * nrm, 0.5) appears twice in the reference's law; one value */
+  const double sq = pow(ijRad * nrm, 0.5);
   double fN = 0.0;
   int st;
   if (nrm < h.plstDfm) st = 1;
@@ -155,12 +157,12 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
   } else if (st == 2) {
     bool elastic = c.hertz_le ? (nrm <= cal.ydsp_t * ijRad) : (nrm < (cal.ydsp_t * ijRad));
     if (elastic) {
-      fN = 4.0 / 3.0 * cal.emod * pow(ijRad * nrm, 0.5) * nrm;
+      fN = 4.0 / 3.0 * cal.emod * sq * nrm;
       h.plstRad = ijRad;
       h.plstDfm = 0.0;
     } else {
       fN = cal.yforce_t * pow(ijRad, 2.0) + cal.ystiff_t * ijRad * (nrm - cal.ydsp_t * ijRad);
-      h.plstRad = ijRad * (4.0 / 3.0 * cal.emod * pow(ijRad * nrm, 0.5) * nrm) / fN;
+      h.plstRad = ijRad * (4.0 / 3.0 * cal.emod * sq * nrm) / fN;
       h.plstDfm = nrm - pow((fN / (4.0 / 3.0 * cal.emod * pow(ijRad, 0.5))), 2.0 / 3.0);
     }
     h.nDsp_mx = nrm;
@@ -171,7 +173,7 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
 
   const double vn = dot3(cpv, u);
   double fD = 0.0;
-  if (c.damp_on) fD = -2.0 * sqrt(c.dmp_sq) * cal.emod * sqrt(ijRad * nrm) * vn;
+  if (c.damp_on) fD = -2.0 * c.dmp * cal.emod * sqrt(ijRad * nrm) * vn;
 
   const double3 vt = sub3(cpv, smul3(vn, u));
   const double3 old = h.dispt;
@@ -182,7 +184,7 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
     dT = add3(dT, mul3(vt, dt));
 
   const double dsmx = 3.0 * cal.sfrc * fN /
-                      (16.0 * (1 - cal.pois) * cal.emod / (4.0 - 2.0 * cal.pois) * pow(ijRad * nrm, 0.5));
+                      (16.0 * (1 - cal.pois) * cal.emod / (4.0 - 2.0 * cal.pois) * sq);
   double ratio = 1.0;
   if (len3(dT) < dsmx) {
     if (dsmx > c.dsmx_eps) ratio = 1.0 - pow((1.0 - len3(dT) / dsmx), 1.5);
