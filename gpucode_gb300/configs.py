@@ -282,14 +282,22 @@ def dry(n: int = 5000, cyl_r: float = 8e-3, seed: int = 1, steps: int = 20000, d
 
 def wet(n: int = 200_000, cyl_r: float = 25e-3, seed: int = 2, steps: int = 50000, dt: float = 5e-7,
         n_levels: int = 4, skin_d: float = 1e-4, bridge_frac: float = 0.0125, gravity: float = 0.0,
-        deposit_tries: int = 8) -> Workload:
-    """Wet polydisperse packing: log-normal sizes, capillary bridges, deposited bed."""
+        deposit_tries: int = 8, packing: str = "deposit") -> Workload:
+    """Wet polydisperse packing: log-normal sizes, capillary bridges, deposited bed
+    (packing="lattice": the spheres on a hexagonal lattice spaced 5 % wider than
+    the largest diameter instead, apart from one another; seconds to build at
+    any size)."""
     dia = lognormal_diameters(n, 1e-3, 0.2, 0.5e-3, 2.0e-3, seed)
     real = 2.0e-3  # REALSIZE: the largest admissible diameter
     rmin, rmax = dia.min() / 2, dia.max() / 2
     yldp = yldp_for_yield_overlap(0.01, E_YOUNG, NU)
     dmpn = calibrate_dmpn(0.7, 0.5, 1e-3, RHO, E_YOUNG, NU, yldp)
-    pos = deposit(dia, cyl_r, 0.0, 0.0, deposit_tries, seed)
+    if packing == "deposit":
+        pos = deposit(dia, cyl_r, 0.0, 0.0, deposit_tries, seed)
+    elif packing == "lattice":
+        pos = hex_lattice(n, real, cyl_r, 0.0, 1.05 * real, 0.0, seed)
+    else:
+        raise ValueError(f"packing must be 'deposit' or 'lattice', not {packing!r}")
     top = float((pos[:, 2] + dia / 2).max())
     cut_gap = (skin_d / real) * rmax / rmin
     inp = make_input(n, n_levels, real, cut_gap, cyl_r, top + 10 * real, RHO, E_YOUNG, NU, MU, dmpn, yldp, 1,

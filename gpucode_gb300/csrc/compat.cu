@@ -304,9 +304,13 @@ void PpInterCalc(double3* pos, double3* vel, double3* angvel, double* rad, int* 
                  int* d_Num_Nebor, int* d_lqdCnt, int* d_lqdCnt_Old, double3* force, double3* mom, double* rmom,
                  int TotalParticle, int NP, int ForceCap, int stage) {
   (void)NP;
+  /* the spheres' liquid shares go to the library's scratch (the neighbour
+   * build's sort scratch, idle between builds on the same stream) */
+  double* share = ForceCap == 1 ? static_cast<double*>(ensure_scratch((size_t)TotalParticle * sizeof(double)))
+                                : nullptr;
   ok_or_exit(dem::pp_force64(pos, vel, angvel, rad, d_Nebor1, d_pLevel, d_level_nPars, d_level_nNebors,
                              d_Nebor_Idx, soa(h), d_Num_Nebor, d_lqdCnt, d_lqdCnt_Old, force, mom, rmom,
-                             TotalParticle, ForceCap, stage, g_consts, nullptr, 0));
+                             TotalParticle, ForceCap, stage, g_consts, nullptr, share, 0));
 }
 
 void CirPWCalc(double3* pos, double3* vel, double3* angvel, double3* force, double3* mom, double* rmom, double* rad,

@@ -167,7 +167,7 @@ dem_status pp_force64(const double3* pos, const double3* vel, const double3* ang
                       const int* level_npars, const int* level_nnebors, const int* nebor_idx,
                       H h, const int* num_nebor, int* lqd, const int* lqd_old,
                       double3* force, double3* mom, double* rmom, int n, int force_cap, int stage,
-                      const DevConsts& k, unsigned long long* counters, cudaStream_t stream,
+                      const DevConsts& k, unsigned long long* counters, double* pvol, cudaStream_t stream,
                       const int* id = nullptr, LiquidModel lm = LiquidModel{0, 0.f, 0.0, 0.0, 0ull});
 /* CirPWInterG (kernel.cu:958-1023).  move_wall: advance the top wall first
  * (the reference's particle-0 thread does this inside the kernel). */

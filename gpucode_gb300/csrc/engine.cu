@@ -403,9 +403,10 @@ dem_status enqueue_step(dem_ctx* c, cudaStream_t s, int parity) {
   if (c->opt.precision == DEM_PREC_MIXED) return mixed_step(c, parity, s);
   dem_status st = var_init(b.force, b.mom, b.rmom, b.lqd, b.lqd_old, n, s);
   if (st != DEM_OK) return st;
+  /* the export staging is idle during a step: it holds the spheres' liquid shares */
   st = pp_force64<HistAoS>(b.pos, b.vel, b.angv, b.rad, b.nebor, b.plevel, b.npars, b.nneb, b.nidx, hist_pp(c),
                            b.num_nebor, b.lqd, b.lqd_old, b.force, b.mom, b.rmom, n, c->s.force_cap,
-                           c->s.load_stage, c->k, b.counters, s, b.id, c->lm);
+                           c->s.load_stage, c->k, b.counters, reinterpret_cast<double*>(b.tmp_out), s, b.id, c->lm);
   if (st != DEM_OK) return st;
   st = wall_force64<HistAoS>(b.pos, b.vel, b.angv, b.force, b.mom, b.rmom, b.rad, b.cyl, hist_pw(c), b.nwall,
                              b.wlist, 3 * sizeof(int), n, n, c->s.load_stage, c->k, b.counters,

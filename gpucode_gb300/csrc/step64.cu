@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(128) k_pp_force64(
     const int* __restrict__ nebor_idx, HA h, const int* __restrict__ num_nebor, int* __restrict__ lqd,
     const int* __restrict__ lqd_old, double3* __restrict__ force, double3* __restrict__ mom,
     double* __restrict__ rmom, int n, int force_cap, int stage, DevConsts k,
-    unsigned long long* __restrict__ counters, const int* __restrict__ id, LiquidModel lm) {
+    unsigned long long* __restrict__ counters, const int* __restrict__ id, LiquidModel lm,
+    const double* __restrict__ pvol) {
   /* blocks in reverse: in cell order the largest spheres, with the most
    * pairs, come last (in the reference's order this is only another schedule) */
   const int i = reversed_block_thread();
@@ -63,9 +64,8 @@ __global__ void __launch_bounds__(128) k_pp_force64(
 
   const double3 ip = pos[i], iv = vel[i], iw = angvel[i];
   const double ir = rad[i];
-  int inl = lqd_old[i];
-  if (inl < 12) inl = 12;
-  const double iVol = k.lqd.vol * pow((ir * 2), 3.0) / inl;
+  const bool ref_liquid = force_cap == 1 && lm.mode == 0;
+  const double iVol = ref_liquid ? pvol[i] : 0.0;
   double3 F = force[i];
   double3 M = mom[i];
   double R = rmom[i];
@@ -113,10 +113,8 @@ __global__ void __launch_bounds__(128) k_pp_force64(
     const bool film = gap < 2 * k.lqd.layer * (ir + jr);
     if (!film && brg0 == 0) continue;
     int brg = brg0;
-    if (lm.mode == 0) {
-      int jnl = lqd_old[j];
-      if (jnl < 12) jnl = 12;
-      const double jVol = k.lqd.vol * pow((jr * 2), 3.0) / jnl;
+    if (ref_liquid) {
+      const double jVol = pvol[j];
       double ijVol = iVol + jVol;
       if (film) brg = 1;
       else if (gap > 0.99 * pow(ijVol, 0.33)) brg = 0;
@@ -165,6 +163,18 @@ __global__ void __launch_bounds__(128) k_pp_force64(
 /* CirPWInterG (kernel.cu:958-1023).  The reference's particle-0 thread moves
  * the top wall while other threads read it; here a one-thread launch moves it
  * first and every particle sees the moved wall. */
+/* each sphere's share of liquid, vol (2r)^3 / max(bridges last step, 12)
+ * (kernel.cu:429-434, :511-518): a per-sphere value the reference recomputes for
+ * every neighbour entry; computed once here by the same operations */
+__global__ void k_liquid_share(const double* __restrict__ rad, const int* __restrict__ lqd_old,
+                               double* __restrict__ pvol, int n, DevConsts k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int nl = lqd_old[i];
+  if (nl < 12) nl = 12;
+  pvol[i] = k.lqd.vol * pow((rad[i] * 2), 3.0) / nl;
+}
+
 __global__ void k_move_top_wall(CylinderBC* cyl, double dt) {
   if (blockIdx.x == 0 && threadIdx.x == 0) cyl->Tw = cyl->Tw + cyl->topv * dt;
 }
@@ -289,14 +299,18 @@ dem_status pp_force64(const double3* pos, const double3* vel, const double3* ang
                       const int* nebor, const int* plevel, const int* level_npars, const int* level_nnebors,
                       const int* nebor_idx, H h, const int* num_nebor, int* lqd, const int* lqd_old,
                       double3* force, double3* mom, double* rmom, int n, int force_cap, int stage,
-                      const DevConsts& k, unsigned long long* counters, cudaStream_t stream, const int* id,
-                      LiquidModel lm) {
+                      const DevConsts& k, unsigned long long* counters, double* pvol, cudaStream_t stream,
+                      const int* id, LiquidModel lm) {
   if (n <= 0) return DEM_OK;
   using HA = typename Acc<H>::T;
+  if (force_cap == 1 && lm.mode == 0) {
+    if (!pvol) return fail(DEM_ERR_ARG, "pp_force64: the liquid shares need an n-double scratch array");
+    k_liquid_share<<<grid_for(n, 256), 256, 0, stream>>>(rad, lqd_old, pvol, n, k);
+  }
   k_pp_force64<HA><<<grid_for(n, 128), 128, 0, stream>>>(pos, vel, angvel, rad, nebor, plevel, level_npars,
                                                         level_nnebors, nebor_idx, Acc<H>::make(h), num_nebor, lqd,
                                                         lqd_old, force, mom, rmom, n, force_cap, stage, k,
-                                                        counters, id, lm);
+                                                        counters, id, lm, pvol);
   return cuda_check(cudaGetLastError(), "pp_force64 launch");
 }
 
@@ -318,11 +332,11 @@ dem_status wall_force64(const double3* pos, const double3* vel, const double3* a
 template dem_status pp_force64<HistSoA>(const double3*, const double3*, const double3*, const double*, const int*,
                                         const int*, const int*, const int*, const int*, HistSoA, const int*, int*,
                                         const int*, double3*, double3*, double*, int, int, int, const DevConsts&,
-                                        unsigned long long*, cudaStream_t, const int*, LiquidModel);
+                                        unsigned long long*, double*, cudaStream_t, const int*, LiquidModel);
 template dem_status pp_force64<HistAoS>(const double3*, const double3*, const double3*, const double*, const int*,
                                         const int*, const int*, const int*, const int*, HistAoS, const int*, int*,
                                         const int*, double3*, double3*, double*, int, int, int, const DevConsts&,
-                                        unsigned long long*, cudaStream_t, const int*, LiquidModel);
+                                        unsigned long long*, double*, cudaStream_t, const int*, LiquidModel);
 template dem_status wall_force64<HistSoA>(const double3*, const double3*, const double3*, double3*, double3*,
                                           double*, const double*, CylinderBC*, HistSoA, const int*, const int*,
                                           size_t, int, int, int, const DevConsts&, unsigned long long*, bool,

@@ -81,3 +81,40 @@ def test_fitted_slots_give_the_same_run(cuda):
     np.testing.assert_array_equal(a.get_state()["pos"], b.get_state()["pos"])
     for e in (a, b):
         e.close()
+
+
+@pytest.mark.gpu
+def test_sixteen_million_spheres_fit_180_gb(cuda):
+    """The 16,000,000-sphere wet set-up (R = 150 mm, four levels): at the
+    reference's slot counts it needs more than 180 GB; fitted to 180 GB the
+    engine is created within the estimate, takes the state and steps without a
+    slot overflow, and a lattice of spheres apart from one another comes back
+    through the permutation to cell order and back with x and y unchanged
+    (nothing pushes sideways) and every sphere a little lower (gravity)."""
+    import torch
+
+    from gpucode_gb300 import configs
+
+    w = configs.wet(n=16_000_000, cyl_r=0.15, packing="lattice")
+    assert w.setup.memory("mixed")["total"] > 180e9
+    f = w.setup.fit_memory(180e9, min_slots=8, precision="mixed")
+    est = w.setup.memory("mixed")["total"]
+    assert f < 1.0 and est <= 180e9
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    if free0 < est + 2e9:
+        pytest.skip(f"{free0 / 1e9:.0f} GB free on the device, {est / 1e9:.0f} GB needed")
+    eng = Engine(w.setup, precision="mixed")
+    torch.cuda.synchronize()
+    used = free0 - torch.cuda.mem_get_info()[0]
+    assert used <= est, (used, est)
+    pos = w.pos0_reduced
+    eng.set_state(pos)
+    eng.step(20)
+    eng.sync()  # raises on a slot overflow
+    st = eng.get_state()
+    eng.close()
+    np.testing.assert_array_equal(st["pos"][:, :2], pos[:, :2])
+    assert not st["vel"][:, :2].any()
+    drop = pos[:, 2] - st["pos"][:, 2]
+    assert (drop > 0).all() and (drop < 1e-5).all(), (drop.min(), drop.max())
