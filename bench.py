@@ -1122,10 +1122,11 @@ def reference_kernels(w, args, flush, value, closure, kernel_ms) -> dict:
     except RuntimeError as ex:
         return {"unavailable": str(ex)}
     rv = n / (r["step_ms"] * 1e-3)
-    drop_in = drop_in_path(w, stt, args, flush)
-    if "value" in drop_in:
-        drop_in["vs_reference_kernels"] = drop_in["value"] / rv
-    return {"value": rv, "unit": UNIT, "ms_per_step": r["step_ms"], "drop_in_path": drop_in,
+    drop_in = {p: drop_in_path(w, stt, args, flush, p) for p in ("fp64", "mixed")}
+    for d in drop_in.values():
+        d["vs_reference_kernels"] = d["value"] / rv
+    return {"value": rv, "unit": UNIT, "ms_per_step": r["step_ms"], "drop_in_path": drop_in["fp64"],
+            "drop_in_path_mixed": drop_in["mixed"],
             "kernel_ms": {"PPForceCalcG": r["force_ms"], "CirPWInterG": r["wall_ms"],
                           "UpdateSystemG": r["update_ms"]},
             "rebuilds": r["rebuilds"], "slot_overflow": bool(r["overflow"]), "speedup": value / rv,
@@ -1136,12 +1137,13 @@ def reference_kernels(w, args, flush, value, closure, kernel_ms) -> dict:
                       "read, VarInit memsets)"}
 
 
-def drop_in_path(w, stt, args, flush) -> dict:
+def drop_in_path(w, stt, args, flush, precision: str) -> dict:
     """the reference's API driven in main.cpp's order (gpucode_gb300.dropin:
-    what the reference's unchanged main.cpp gets from this library, the FP64
-    kernels) from the same state as the reference's kernels, timed the same
-    way: L2 evicted before each step, CUDA events around it, the per-step flag
-    read included"""
+    what the reference's unchanged main.cpp gets from this library; "fp64"
+    the default FP64 kernels, "mixed" what DEM_COMPAT_PRECISION=mixed selects)
+    from the same state as the reference's kernels, timed the same way: L2
+    evicted before each step, CUDA events around it, the per-step flag read
+    included"""
     import ctypes as C
 
     import torch
@@ -1151,24 +1153,29 @@ def drop_in_path(w, stt, args, flush) -> dict:
 
     n = w.setup.n
     drv = DropInDriver(w, stt["pos"], stt["vel"], stt["angvel"], torch)
-    for _ in range(5):
-        drv.step()
-    torch.cuda.synchronize()
     lib = drv.lib
-    tot, rebuilds = 0.0, 0
-    for _ in range(args.ref_gpu_steps):
-        check(lib.dem_l2_flush(None, C.c_void_p(flush.data_ptr()), flush.numel()), "dem_l2_flush")
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record()
-        rebuilds += int(drv.step())
-        b.record()
-        b.synchronize()
-        tot += a.elapsed_time(b)
+    check(lib.dem_compat_set_precision(1 if precision == "mixed" else 0), "dem_compat_set_precision")
+    try:
+        for _ in range(5):
+            drv.step()
+        torch.cuda.synchronize()
+        tot, rebuilds = 0.0, 0
+        for _ in range(args.ref_gpu_steps):
+            check(lib.dem_l2_flush(None, C.c_void_p(flush.data_ptr()), flush.numel()), "dem_l2_flush")
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            rebuilds += int(drv.step())
+            b.record()
+            b.synchronize()
+            tot += a.elapsed_time(b)
+    finally:
+        check(lib.dem_compat_set_precision(0), "dem_compat_set_precision")
     ms = tot / args.ref_gpu_steps
     return {"value": n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "rebuilds": rebuilds,
+            "precision": precision,
             "sample": f"{args.ref_gpu_steps} steps after 5 warm-up, the same state and method as the reference's "
-                      "kernels (the FP64 kernels behind heydem.h's API, main.cpp's step order)"}
+                      f"kernels ({precision} kernels behind heydem.h's API, main.cpp's step order)"}
 
 
 if __name__ == "__main__":

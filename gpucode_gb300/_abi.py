@@ -250,6 +250,8 @@ def _declare(lib: C.CDLL) -> None:
         "dem_packing_metrics": (I, [I, P, P, P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(I)]),
         "dem_l2_flush": (I, [P, P, C.c_size_t]),
         "dem_compat_errors": (I, []),
+        "dem_compat_set_precision": (I, [I]),
+        "dem_compat_precision": (I, []),
         "dem_set_systems": (I, [P, I, P, P, P]),
         "dem_profile_kernels": (I, [P, P, I, C.POINTER(I)]),
         "dem_scale_cells": (I, [C.POINTER(DemSetup), C.c_double]),

@@ -46,6 +46,19 @@ struct CompatDevice {
 };
 CompatDevice g_dev;
 
+/* the arithmetic of PpInterCalc / CirPWCalc / UpdateSystem: DEM_PREC_FP64 (the
+ * reference's) unless DEM_COMPAT_PRECISION=mixed is set in the environment or
+ * dem_compat_set_precision chose otherwise; -1 until first asked */
+int g_precision = -1;
+
+int compat_precision() {
+  if (g_precision < 0) {
+    const char* e = std::getenv("DEM_COMPAT_PRECISION");
+    g_precision = (e && std::strcmp(e, "mixed") == 0) ? DEM_PREC_MIXED : DEM_PREC_FP64;
+  }
+  return g_precision;
+}
+
 void ensure_small() {
   if (!g_dev.err) {
     DEM_REF_CHECK(cudaMalloc((void**)&g_dev.err, sizeof(int)));
@@ -102,6 +115,15 @@ extern "C" {
 
 /* reads and clears the compat path's device error word: bit 1 = neighbour-slot
  * overflow, bit 4 = a particle hashed outside the cell grid */
+dem_status dem_compat_set_precision(int precision) {
+  if (precision != DEM_PREC_FP64 && precision != DEM_PREC_MIXED)
+    return dem::fail(DEM_ERR_ARG, "dem_compat_set_precision: DEM_PREC_FP64 or DEM_PREC_MIXED");
+  g_precision = precision;
+  return DEM_OK;
+}
+
+int dem_compat_precision(void) { return compat_precision(); }
+
 int dem_compat_errors(void) {
   if (!g_dev.err) return 0;
   int v = 0;
@@ -304,6 +326,12 @@ void PpInterCalc(double3* pos, double3* vel, double3* angvel, double* rad, int* 
                  int* d_Num_Nebor, int* d_lqdCnt, int* d_lqdCnt_Old, double3* force, double3* mom, double* rmom,
                  int TotalParticle, int NP, int ForceCap, int stage) {
   (void)NP;
+  if (compat_precision() == DEM_PREC_MIXED) {
+    ok_or_exit(dem::pp_force_ref_mixed(pos, vel, angvel, rad, d_Nebor1, d_pLevel, d_level_nPars, d_level_nNebors,
+                                       d_Nebor_Idx, soa(h), d_Num_Nebor, d_lqdCnt, d_lqdCnt_Old, force, mom, rmom,
+                                       TotalParticle, ForceCap, stage, g_consts, 0));
+    return;
+  }
   /* the spheres' liquid shares go to the library's scratch (the neighbour
    * build's sort scratch, idle between builds on the same stream) */
   double* share = ForceCap == 1 ? static_cast<double*>(ensure_scratch((size_t)TotalParticle * sizeof(double)))
@@ -316,6 +344,11 @@ void PpInterCalc(double3* pos, double3* vel, double3* angvel, double* rad, int* 
 void CirPWCalc(double3* pos, double3* vel, double3* angvel, double3* force, double3* mom, double* rmom, double* rad,
                CylinderBC* d_Cir, PWCONTACT_HISTORY h, int* d_Num_StlWall, int* d_StlW_List, size_t pitch_Sw1,
                int TotalParticle, int NP, int stage) {
+  if (compat_precision() == DEM_PREC_MIXED) {
+    ok_or_exit(dem::wall_force_ref_mixed(pos, vel, angvel, force, mom, rmom, rad, d_Cir, soa(h), d_Num_StlWall,
+                                         d_StlW_List, pitch_Sw1, TotalParticle, NP, stage, g_consts, 0));
+    return;
+  }
   ok_or_exit(dem::wall_force64(pos, vel, angvel, force, mom, rmom, rad, d_Cir, soa(h), d_Num_StlWall, d_StlW_List,
                                pitch_Sw1, TotalParticle, NP, stage, g_consts, nullptr, true, 0));
 }
@@ -323,7 +356,7 @@ void CirPWCalc(double3* pos, double3* vel, double3* angvel, double3* force, doub
 void UpdateSystem(double* rad, double3* pos, double3* vel, double3* angvel, double3* force, double3* mom,
                   double* rmom, int* d_ReNebld, double* d_pMoveforReBld, int TotalParticle) {
   ok_or_exit(dem::update64(rad, pos, vel, angvel, force, mom, rmom, d_ReNebld, d_pMoveforReBld, TotalParticle,
-                           g_consts, 0));
+                           g_consts, 0, compat_precision() == DEM_PREC_FP64));
 }
 
 void NeborToCPU(int* h_Num_Nebor, int* d_Num_Nebor, int* h_1DNebor, int* d_Nebor1, int* h_Num_stlWall,

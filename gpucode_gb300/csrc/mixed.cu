@@ -1418,6 +1418,211 @@ Law32 make_law(const calParaPP& c, bool pp, double dmp_sq, int stage) {
   return l;
 }
 
+
+/* ---- the reference's entry points in mixed precision ----
+ * PpInterCalc and CirPWCalc (kernel.cu:413-552, :958-1023) on the reference's
+ * own layouts -- spheres in the caller's order, level/slot-major lists, FP64
+ * SoA histories -- with the fused step's FP32 laws: a pair's overlap from the
+ * FP64 positions as (d^2 - S^2) / (d + S) with d^2 - S^2 in FP64 (six FP64
+ * operations, no FP64 square root, division or pow), the contact law and
+ * the bridge in FP32, the sums in Kahan FP32 added to the FP64 force arrays.
+ * The histories keep the spring and the peak overlap in FP64, as the fused
+ * step does; the re-derived fields are written back as FP64 copies of FP32
+ * values. */
+struct RefArrays {
+  const double3 *pos, *vel, *angv;
+  const double* rad;
+  const int *nebor, *plevel, *npars, *nneb, *nidx, *num_nebor, *lqd_old;
+  int* lqd;
+  HistSoA h;
+  double3 *force, *mom;
+  double* rmom;
+  /* walls */
+  const CylinderBC* cyl;
+  const int *nwall, *wlist;
+  size_t pitch;
+  int np;
+};
+
+__device__ __forceinline__ float3 d2f3(double3 v) { return f3(d2f(v.x), d2f(v.y), d2f(v.z)); }
+
+__device__ __forceinline__ MixedRec soa_load(const HistSoA& h, long long s) {
+  MixedRec r;
+  const double3 d = h.dispt[s];
+  r.dx = d.x;
+  r.dy = d.y;
+  r.dz = d.z;
+  r.nDsp_mx = h.nDsp_mx[s];
+  r.fx = d2f(d.x);
+  r.fy = d2f(d.y);
+  r.fz = d2f(d.z);
+  r.nDsp = d2f(h.nDsp[s]);
+  r.plstRad = d2f(h.plstRad[s]);
+  r.plstDfm = d2f(h.plstDfm[s]);
+  r.stage = h.stage[s];
+  r.pad = 0;
+  return r;
+}
+__device__ __forceinline__ void soa_store(const HistSoA& h, long long s, const MixedRec& r) {
+  h.dispt[s] = make_double3(r.dx, r.dy, r.dz);
+  h.nDsp_mx[s] = r.nDsp_mx;
+  h.nDsp[s] = f2d(r.nDsp);
+  h.plstRad[s] = f2d(r.plstRad);
+  h.plstDfm[s] = f2d(r.plstDfm);
+  h.stage[s] = r.stage;
+}
+
+/* adds sums to an FP64 triple */
+__device__ __forceinline__ double3 add_sum(double3 v, const KSum3& s) {
+  return make_double3(v.x + f2d(s.x.s - s.x.c), v.y + f2d(s.y.s - s.y.c), v.z + f2d(s.z.s - s.z.c));
+}
+
+__global__ void __launch_bounds__(128) k_pp_ref_mixed(MixArgs a, RefArrays r) {
+  const int i = reversed_block_thread();
+  if (i >= a.n) return;
+  const double3 ip = r.pos[i];
+  const double ird = r.rad[i];
+  const float ri = d2f(ird);
+  const float3 iv = d2f3(r.vel[i]), iw = d2f3(r.angv[i]);
+  const bool wet_i = a.force_cap == 1;
+  float iVol = 0.f;
+  if (wet_i) {
+    const int inl = max(r.lqd_old[i], 12);
+    const float ti = 2.0f * ri;
+    iVol = __fdividef(a.lqd_vol * (ti * ti * ti), (float)inl);
+  }
+  KSum3 F, M;
+  KSum R;
+  int wet = 0;
+  const int L = r.plevel[i];
+  const long long stride = r.npars[L];
+  const long long base = slot_base(L, r.npars, r.nneb) + r.nidx[i];
+  const int nn = r.num_nebor[i];
+  for (int k = 0; k < nn; k++) {
+    const long long s = base + k * stride;
+    const int j = r.nebor[s];
+    const double3 jp = r.pos[j];
+    const double jrd = r.rad[j];
+    const double dx = ip.x - jp.x, dy = ip.y - jp.y, dz = ip.z - jp.z;
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const double S = ird + jrd;
+    const double D = d2 - S * S;
+    if (!wet_i && D >= 0.0) continue; /* apart: nothing to do on a dry bed */
+    const float dist = sqrtf(d2f(d2));
+    const float rj = d2f(jrd);
+    const float gap = __fdividef(d2f(D), dist + d2f(S));
+    const float inv = __frcp_rn(dist);
+    const float3 u = f3(d2f(dx) * inv, d2f(dy) * inv, d2f(dz) * inv);
+    if (gap < 0.f) {
+      MixedRec rc = soa_load(r.h, s);
+      const float3 vj = d2f3(r.vel[j]), wj = d2f3(r.angv[j]);
+      const float3 cpv = (iv - vj) - crossf(iw * ri + wj * rj, u);
+      float3 dF, dM;
+      float dR;
+      law32(a.pp, ri * rj / (ri + rj), -gap, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
+      soa_store(r.h, s, rc);
+      F.add(dF);
+      M.add(dM);
+      R.add(dR);
+    }
+    if (!wet_i) continue;
+    const int bprev = r.h.lqdBrg[s];
+    const bool form = gap < 2.0f * a.lqd_layer * (ri + rj);
+    if (!form && bprev == 0) continue;
+    const int jnl = max(r.lqd_old[j], 12);
+    const float tj = 2.0f * rj;
+    const float ijVol = iVol + __fdividef(a.lqd_vol * (tj * tj * tj), (float)jnl);
+    int b = bprev;
+    if (form) b = 1;
+    else if (gap > bridge_rupture32(a, ijVol, 0.f)) b = 0;
+    if (b != bprev) r.h.lqdBrg[s] = b;
+    if (b == 1) {
+      const float fc = bridge_force32(a, gap < 0.f ? 0.f : gap, ijVol, 0.f, 2.0f * ri * rj / (ri + rj));
+      F.add(u * (-fc));
+      wet++;
+    }
+  }
+  double3 f = add_sum(r.force[i], F);
+  const double t = 2.0 * ird;
+  f.z = f.z - t * t * t; /* gravity, m = (2r)^3 */
+  r.force[i] = f;
+  r.mom[i] = add_sum(r.mom[i], M);
+  r.rmom[i] = r.rmom[i] + f2d(R.s - R.c);
+  if (wet_i) r.lqd[i] = r.lqd[i] + wet;
+}
+
+/* CirPWInterG on the reference's wall lists (row i of pitch bytes) and wall
+ * histories (slot a * NP + i); the wall point in FP64 as the fused step
+ * takes it, the law in FP32.  The top wall has moved before this launch. */
+__global__ void __launch_bounds__(128) k_wall_ref_mixed(MixArgs a, RefArrays r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int nw = r.nwall[i];
+  if (nw <= 0) return;
+  const CylinderBC cy = *r.cyl;
+  const double3 p = r.pos[i];
+  const double rid = r.rad[i];
+  const float ri = d2f(rid);
+  const float3 iv = d2f3(r.vel[i]), iw = d2f3(r.angv[i]);
+  const int* row = reinterpret_cast<const int*>(reinterpret_cast<const char*>(r.wlist) + (size_t)i * r.pitch);
+  KSum3 F, M;
+  KSum R;
+  float3 jv = f3(0.f, 0.f, 0.f); /* persists across walls (kernel.cu:980) */
+  for (int w = 0; w < nw; w++) {
+    const int kind = row[w];
+    double3 jp;
+    if (kind == 0) {
+      jp = make_double3(p.x, p.y, cy.Tw);
+      jv = f3(0.f, 0.f, d2f(cy.topv));
+    } else if (kind == 1) {
+      jp = make_double3(p.x, p.y, cy.Bw);
+    } else if (kind == 2) {
+      const double ddx = cy.cir.x - p.x, ddy = cy.cir.y - p.y;
+      const double dist = sqrt(ddx * ddx + ddy * ddy);
+      jp = make_double3(cy.R * ((p.x - cy.cir.x) / dist) + cy.cir.x, cy.R * ((p.y - cy.cir.y) / dist) + cy.cir.y,
+                        p.z);
+    } else {
+      continue;
+    }
+    const double3 d = make_double3(p.x - jp.x, p.y - jp.y, p.z - jp.z);
+    const double len = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+    const float gapw = d2f(len - rid);
+    if (gapw >= 0.f) continue;
+    const float il = __frcp_rn(d2f(len));
+    const float3 u = f3(d2f(d.x) * il, d2f(d.y) * il, d2f(d.z) * il);
+    const float3 cpv = (iv - jv) - crossf(iw * ri, u);
+    const long long s = (long long)w * r.np + i;
+    MixedRec rc = soa_load(r.h, s);
+    float3 dF, dM;
+    float dR;
+    law32(a.pw, ri, -gapw, u, cpv, rc, ri, a.rfrc, a.dtf, dF, dM, dR);
+    soa_store(r.h, s, rc);
+    F.add(dF);
+    M.add(dM);
+    R.add(dR);
+  }
+  r.force[i] = add_sum(r.force[i], F);
+  r.mom[i] = add_sum(r.mom[i], M);
+  r.rmom[i] = r.rmom[i] + f2d(R.s - R.c);
+}
+
+MixArgs ref_args(const DevConsts& k, int n, int force_cap, int stage) {
+  MixArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.n = n;
+  a.force_cap = force_cap;
+  a.dt = k.prm.dt;
+  a.dtf = (float)k.prm.dt;
+  a.rfrc = (float)k.mat[0].rfrc;
+  a.lqd_vol = (float)k.lqd.vol;
+  a.lqd_layer = (float)k.lqd.layer;
+  a.lqd_gapmn = (float)k.lqd.gapmn;
+  a.lqd_st = (float)k.lqd.stension;
+  a.pp = make_law(k.cal, true, k.mat[0].dmpn * k.mat[0].dmpn, stage);
+  a.pw = make_law(k.pwcal, false, k.mat[0].dmpn * k.mat[1].dmpn, stage);
+  a.lq_mode = 0;
+  return a;
+}
 }  // namespace
 
 #ifndef DEM_COOP_CARVEOUT
@@ -1604,6 +1809,37 @@ dem_status mixed_force_to_master(dem_ctx* c, cudaStream_t s) {
   /* the bridge counts of the last step live in the shadow the next step reads */
   k_lqd_from_shadow<<<grid_for(c->n, 256), 256, 0, s>>>(c->n, c->mx->vel[c->parity], c->b.lqd);
   return cuda_check(cudaGetLastError(), "mixed_force_to_master launch");
+}
+
+dem_status pp_force_ref_mixed(const double3* pos, const double3* vel, const double3* angvel, const double* rad,
+                              const int* nebor, const int* plevel, const int* level_npars, const int* level_nnebors,
+                              const int* nebor_idx, HistSoA h, const int* num_nebor, int* lqd, const int* lqd_old,
+                              double3* force, double3* mom, double* rmom, int n, int force_cap, int stage,
+                              const DevConsts& k, cudaStream_t s) {
+  if (n <= 0) return DEM_OK;
+  RefArrays r;
+  std::memset(&r, 0, sizeof(r));
+  r.pos = pos; r.vel = vel; r.angv = angvel; r.rad = rad;
+  r.nebor = nebor; r.plevel = plevel; r.npars = level_npars; r.nneb = level_nnebors; r.nidx = nebor_idx;
+  r.num_nebor = num_nebor; r.lqd_old = lqd_old; r.lqd = lqd; r.h = h;
+  r.force = force; r.mom = mom; r.rmom = rmom;
+  k_pp_ref_mixed<<<grid_for(n, 128), 128, 0, s>>>(ref_args(k, n, force_cap, stage), r);
+  return cuda_check(cudaGetLastError(), "pp_force_ref_mixed launch");
+}
+
+dem_status wall_force_ref_mixed(const double3* pos, const double3* vel, const double3* angvel, double3* force,
+                                double3* mom, double* rmom, const double* rad, CylinderBC* cyl, HistSoA h,
+                                const int* nwall, const int* wlist, size_t pitch, int n, int NP, int stage,
+                                const DevConsts& k, cudaStream_t s) {
+  if (n <= 0) return DEM_OK;
+  RefArrays r;
+  std::memset(&r, 0, sizeof(r));
+  r.pos = pos; r.vel = vel; r.angv = angvel; r.rad = rad; r.h = h;
+  r.force = force; r.mom = mom; r.rmom = rmom;
+  r.cyl = cyl; r.nwall = nwall; r.wlist = wlist; r.pitch = pitch; r.np = NP;
+  k_move_walls<<<1, 32, 0, s>>>(cyl, 1, k.prm.dt, nullptr);
+  k_wall_ref_mixed<<<grid_for(n, 128), 128, 0, s>>>(ref_args(k, n, 0, stage), r);
+  return cuda_check(cudaGetLastError(), "wall_force_ref_mixed launch");
 }
 
 }  // namespace dem

@@ -453,6 +453,19 @@ void dem_set_feed_seed(unsigned long long seed);
  * (dem_last_error). */
 int ParticleFeedDevice(FeedZone* Feedcube, CylinderBC* h_Cir, double InitParSize, double3* dPos,
                        double* dRad, int numParticle, int NP, unsigned long long seed);
+/* The arithmetic of the reference-compatible PpInterCalc, CirPWCalc and
+ * UpdateSystem.  DEM_PREC_FP64 (the default): the reference's FP64 formulas,
+ * forces equal to the CPU oracle's to 1e-12.  DEM_PREC_MIXED: the fused step's
+ * FP32 contact and bridge laws on the same layouts (Kahan sums; positions,
+ * velocities, springs and peak overlaps stay FP64; mass and inertia by
+ * multiplications), the tolerances of dem_options.precision = DEM_PREC_MIXED.
+ * The environment variable DEM_COMPAT_PRECISION=mixed selects the mixed mode
+ * for a driver that is not changed (the reference's main.cpp); this call
+ * overrides it.  Lists (BldNeborList) are the same in both modes.
+ * Returns DEM_ERR_ARG for another value. */
+dem_status dem_compat_set_precision(int precision);
+/* the mode the next reference-compatible call will use (DEM_PREC_*) */
+int dem_compat_precision(void);
 /* Reads and clears the error word of the reference-compatible entry points:
  * bit 1 = a neighbour list stopped at its level's slot capacity (the
  * reference would write past it, kernel.cu:833-836), bit 4 = a particle hashed

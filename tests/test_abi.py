@@ -63,3 +63,27 @@ def test_header_compiles_as_c_and_cxx(tmp_path):
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(RuntimeError, match="not built"):
         _abi.load(tmp_path / "libdem_gb300.so")
+
+
+def test_compat_precision_switch():
+    """DEM_COMPAT_PRECISION=mixed selects the mixed mode of the reference's entry
+    points for an unchanged driver; dem_compat_set_precision overrides it and
+    rejects other values (no GPU call: fresh processes, so the environment is
+    read anew)"""
+    import os
+    import sys
+
+    code = ("from gpucode_gb300 import _abi; lib = _abi.load(); print(lib.dem_compat_precision()); "
+            "print(lib.dem_compat_set_precision(7)); print(lib.dem_compat_set_precision(1), "
+            "lib.dem_compat_precision())")
+    env = {k: v for k, v in os.environ.items() if k != "DEM_COMPAT_PRECISION"}
+    for value, first in ((None, "0"), ("mixed", "1"), ("fp64", "0")):
+        e = dict(env)
+        if value:
+            e["DEM_COMPAT_PRECISION"] = value
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, env=e)
+        assert r.returncode == 0, r.stderr
+        lines = r.stdout.split()
+        assert lines[0] == first, (value, r.stdout)
+        assert int(lines[1]) == _abi.DEM_ERR_ARG
+        assert lines[2:] == ["0", "1"]

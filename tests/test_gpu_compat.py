@@ -27,6 +27,8 @@ _declare = declare
 
 
 FP64_TOL = {"force": 1e-12, "pos": 1e-14, "vel": 1e-12, "hist": 1e-12}
+# the mixed engine's per-step tolerances (forces relative to the step's force scale)
+MIXED_TOL = {"force": 2e-5, "pos": 1e-9, "vel": 1e-5, "angvel": 2e-5, "hist": 1e-5}
 
 
 def _snap(drv, sim, w):
@@ -111,6 +113,46 @@ def test_compat_step_loop_matches_oracle(cuda, make):
         _lockstep.compare_step(_snap(drv, sim, w), sim, w, FP64_TOL, f"step {t}")
     assert rebuilds >= 2
     assert _abi.load().dem_compat_errors() == 0
+
+
+@pytest.mark.parametrize("make", [_workloads.small_dry, _workloads.small_wet])
+def test_compat_mixed_step_loop_matches_oracle(cuda, make):
+    """The same loop with the entry points in mixed precision
+    (dem_compat_set_precision(DEM_PREC_MIXED), what DEM_COMPAT_PRECISION=mixed
+    selects for an unchanged main.cpp): sorted order, cell ranges and
+    neighbour slots still bit-exact, forces, state and histories within the
+    mixed engine's tolerances, at most 1 % of stage or bridge labels flipped
+    where FP32 and FP64 round a turning point differently."""
+    import torch
+
+    w = make()
+    lib = _abi.load()
+    _declare(lib)
+    _abi.check(lib.dem_compat_set_precision(1), "dem_compat_set_precision")
+    try:
+        assert lib.dem_compat_precision() == 1
+        pos, vel, ang = _workloads.stirred(w)
+        drv = RefDriver(w, pos, vel, ang, torch)
+        sim = _harness.OracleSim(w.setup, pos, vel, ang)
+        n = w.setup.n
+        g = lambda x: x.detach().cpu().numpy()  # noqa: E731
+        rebuilds = 0
+        for t in range(250):
+            torch.cuda.synchronize()
+            _load_oracle_from(drv, sim)
+            rb = sim.step()
+            ra = drv.step()
+            torch.cuda.synchronize()
+            assert ra == bool(rb), f"rebuild decision differs at step {t}"
+            rebuilds += rb
+            if rb:
+                assert np.array_equal(g(drv.index), sim.arr("index", np.int32, n)), t
+                assert np.array_equal(g(drv.cs), sim.arr("cellStart", np.int32, drv.C)), t
+            _lockstep.compare_step(_snap(drv, sim, w), sim, w, MIXED_TOL, f"step {t}", mismatch_budget=0.01)
+        assert rebuilds >= 2
+        assert lib.dem_compat_errors() == 0
+    finally:
+        _abi.check(lib.dem_compat_set_precision(0), "dem_compat_set_precision")
 
 
 def test_first_step_forces_match_oracle_tightly(cuda):
