@@ -355,8 +355,13 @@ void CirPWCalc(double3* pos, double3* vel, double3* angvel, double3* force, doub
 
 void UpdateSystem(double* rad, double3* pos, double3* vel, double3* angvel, double3* force, double3* mom,
                   double* rmom, int* d_ReNebld, double* d_pMoveforReBld, int TotalParticle) {
+  if (compat_precision() == DEM_PREC_MIXED) {
+    ok_or_exit(dem::update_ref_mixed(rad, pos, vel, angvel, force, mom, rmom, d_ReNebld, d_pMoveforReBld,
+                                     TotalParticle, g_consts, 0));
+    return;
+  }
   ok_or_exit(dem::update64(rad, pos, vel, angvel, force, mom, rmom, d_ReNebld, d_pMoveforReBld, TotalParticle,
-                           g_consts, 0, compat_precision() == DEM_PREC_FP64));
+                           g_consts, 0));
 }
 
 void NeborToCPU(int* h_Num_Nebor, int* d_Num_Nebor, int* h_1DNebor, int* d_Nebor1, int* h_Num_stlWall,

@@ -177,13 +177,12 @@ dem_status wall_force64(const double3* pos, const double3* vel, const double3* a
                         CylinderBC* cyl, H h, const int* nwall, const int* wlist,
                         size_t pitch, int n, int NP, int stage, const DevConsts& k,
                         unsigned long long* counters, bool move_wall, cudaStream_t stream);
-/* UpdateSystemG (kernel.cu:563-606); pow_mass false: mass and inertia by
- * multiplications instead of pow (the reference entry points' mixed mode) */
+/* UpdateSystemG (kernel.cu:563-606) */
 dem_status update64(const double* rad, double3* pos, double3* vel, double3* angvel,
                     const double3* force, const double3* mom, double* rmom, int* flag,
-                    double* pmove, int n, const DevConsts& k, cudaStream_t stream, bool pow_mass = true);
+                    double* pmove, int n, const DevConsts& k, cudaStream_t stream);
 
-/* PpInterCalc / CirPWCalc in mixed precision on the reference's layouts
+/* PpInterCalc / CirPWCalc / UpdateSystem in mixed precision on the reference's layouts
  * (mixed.cu): FP32 laws and bridges with Kahan sums, FP64 positions, springs
  * and peak overlaps; the reference's liquid model.  The wall call moves the
  * top wall first, as wall_force64 with move_wall does. */
@@ -196,6 +195,11 @@ dem_status wall_force_ref_mixed(const double3* pos, const double3* vel, const do
                                 double3* mom, double* rmom, const double* rad, CylinderBC* cyl, HistSoA h,
                                 const int* nwall, const int* wlist, size_t pitch, int n, int NP, int stage,
                                 const DevConsts& k, cudaStream_t s);
+/* UpdateSystemG in the same mode: FP32 increments (mass, inertia, dv, dw,
+ * path length) added to the FP64 state, as the fused step integrates */
+dem_status update_ref_mixed(const double* rad, double3* pos, double3* vel, double3* angvel, const double3* force,
+                            const double3* mom, double* rmom, int* flag, double* pmove, int n, const DevConsts& k,
+                            cudaStream_t s);
 
 /* device-level helpers */
 dem_status inclusive_scan_small(const int* in, int* out, int n, cudaStream_t stream);

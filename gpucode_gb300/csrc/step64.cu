@@ -251,10 +251,6 @@ __global__ void __launch_bounds__(128) k_wall_force64(
 }
 
 /* UpdateSystemG (kernel.cu:563-606) */
-/* POW: mass and inertia by the reference's pow (the FP64 mode); otherwise by
- * multiplications (the mixed mode: the same values to a few ulp, without the
- * two FP64 pow calls per sphere) */
-template <bool POW>
 __global__ void k_update64(const double* __restrict__ rad, double3* __restrict__ pos, double3* __restrict__ vel,
                            double3* __restrict__ angvel, const double3* __restrict__ force,
                            const double3* __restrict__ mom, double* __restrict__ rmom, int* __restrict__ flag,
@@ -262,8 +258,7 @@ __global__ void k_update64(const double* __restrict__ rad, double3* __restrict__
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double r = rad[i];
-  const double t = 2.0 * r;
-  const double mass = POW ? pow(t, 3.0) : t * t * t;
+  const double mass = pow(2.0 * r, 3.0);
   double3 v = vel[i];
   const double3 f = force[i];
   v.x = v.x + f.x * dt / mass;
@@ -273,7 +268,7 @@ __global__ void k_update64(const double* __restrict__ rad, double3* __restrict__
   pos[i] = add3(pos[i], mul3(v, dt));
   const double pm = pmove[i] + len3(v) * dt;
   pmove[i] = pm;
-  const double inert = 0.1 * (POW ? pow(t, 5.0) : t * t * t * t * t);
+  const double inert = 0.1 * pow(2.0 * r, 5.0);
   double3 w = angvel[i];
   const double3 m = mom[i];
   w.x = w.x + m.x * dt / inert;
@@ -353,14 +348,10 @@ template dem_status wall_force64<HistAoS>(const double3*, const double3*, const 
 
 dem_status update64(const double* rad, double3* pos, double3* vel, double3* angvel, const double3* force,
                     const double3* mom, double* rmom, int* flag, double* pmove, int n, const DevConsts& k,
-                    cudaStream_t stream, bool pow_mass) {
+                    cudaStream_t stream) {
   if (n <= 0) return DEM_OK;
-  if (pow_mass)
-    k_update64<true><<<grid_for(n, 256), 256, 0, stream>>>(rad, pos, vel, angvel, force, mom, rmom, flag, pmove, n,
-                                                          k.prm.dt, k.prm.SearchGap);
-  else
-    k_update64<false><<<grid_for(n, 256), 256, 0, stream>>>(rad, pos, vel, angvel, force, mom, rmom, flag, pmove,
-                                                           n, k.prm.dt, k.prm.SearchGap);
+  k_update64<<<grid_for(n, 256), 256, 0, stream>>>(rad, pos, vel, angvel, force, mom, rmom, flag, pmove, n,
+                                                  k.prm.dt, k.prm.SearchGap);
   return cuda_check(cudaGetLastError(), "update64 launch");
 }
 

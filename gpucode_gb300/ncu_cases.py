@@ -14,6 +14,10 @@ them directly, and each case holds a few GB on the device at most.
         for 3 epochs on the bridges of one step, 3 host-launched steps with it
         fused in the step kernel, then the network's inference on `rows`
         bridges: twice on the tcgen05 path, once on the warp tiles
+    python -m gpucode_gb300.ncu_cases dropin [--precision fp64|mixed] [--steps 3]
+        the packed bed through the reference's entry points in main.cpp's
+        order (gpucode_gb300.dropin): `steps` steps, the first one building
+        the lists, in the chosen mode of PpInterCalc / CirPWCalc / UpdateSystem
 """
 from __future__ import annotations
 
@@ -86,9 +90,27 @@ def closure_case(rows: int) -> None:
     net.close()
 
 
+def dropin_case(precision: str, steps: int) -> None:
+    import torch
+
+    from . import configs
+    from ._abi import check
+    from .dropin import DropInDriver
+
+    w = configs.load_bed(BED)
+    z = w.pos0_reduced * 0.0
+    drv = DropInDriver(w, w.pos0_reduced, z, z, torch)
+    check(drv.lib.dem_compat_set_precision(1 if precision == "mixed" else 0), "dem_compat_set_precision")
+    for _ in range(steps):
+        drv.step()
+    torch.cuda.synchronize()
+    print("ok", precision, steps, "steps, compat errors", drv.lib.dem_compat_errors())
+
+
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("case", choices=["step", "closure"])
+    ap.add_argument("case", choices=["step", "closure", "dropin"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--pairs", default="auto", choices=["auto", "warp", "thread"])
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--rows", type=int, default=1_000_000)
@@ -96,6 +118,8 @@ def main(argv=None) -> None:
     a = ap.parse_args(argv)
     if a.case == "step":
         step_case(a.pairs, a.steps, a.io)
+    elif a.case == "dropin":
+        dropin_case(a.precision, a.steps)
     else:
         closure_case(a.rows)
 

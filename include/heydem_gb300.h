@@ -457,8 +457,8 @@ int ParticleFeedDevice(FeedZone* Feedcube, CylinderBC* h_Cir, double InitParSize
  * UpdateSystem.  DEM_PREC_FP64 (the default): the reference's FP64 formulas,
  * forces equal to the CPU oracle's to 1e-12.  DEM_PREC_MIXED: the fused step's
  * FP32 contact and bridge laws on the same layouts (Kahan sums; positions,
- * velocities, springs and peak overlaps stay FP64; mass and inertia by
- * multiplications), the tolerances of dem_options.precision = DEM_PREC_MIXED.
+ * velocities, springs and peak overlaps stay FP64; the integrator adds FP32
+ * increments to them), the tolerances of dem_options.precision = DEM_PREC_MIXED.
  * The environment variable DEM_COMPAT_PRECISION=mixed selects the mixed mode
  * for a driver that is not changed (the reference's main.cpp); this call
  * overrides it.  Lists (BldNeborList) are the same in both modes.
