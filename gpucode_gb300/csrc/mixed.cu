@@ -32,6 +32,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -1325,30 +1326,65 @@ __global__ void k_import_shadows(int n, const int* __restrict__ id, const double
   w4[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
 }
 
-/* the same import from mapped host arrays read in caller order: thread i
- * reads the caller's element i over the host link and writes cell position
- * inv[i] (state, bridge count and shadows) */
+/* the same import from mapped host arrays read in caller order.  A block
+ * walks slices of kImportThreads particles (slice, slice + gridDim.x, ...):
+ * the caller's three arrays of a slice are read over the host link into
+ * registers, staged in shared memory, and each thread scatters its particle
+ * to cell position inv[i] (state, bridge count and shadows) -- while the next
+ * slice's reads are already in flight, so the link stays busy during the
+ * scatter.  16-byte reads where a slice starts 16-byte aligned (a slice of
+ * 256 double3 is 6144 bytes, so all slices share the array's alignment),
+ * else 8-byte reads. */
 constexpr int kImportThreads = 256;
-/* the block's slice of one mapped host array (kImportThreads particles,
- * contiguous) into shared memory with 16-byte loads when it is 16-byte
- * aligned (a slice of 256 double3 is 6144 bytes), else 8-byte loads */
-__device__ __forceinline__ void stage_slice(const double3* __restrict__ h, int n, double* sm) {
-  const long long i0 = (long long)blockIdx.x * kImportThreads;
-  const int cnt = (int)min((long long)kImportThreads, n - i0);
+constexpr int kSliceDoubles = 3 * kImportThreads;
+/* resident import blocks per SM: 4 (or 8) read the 14.4 MB state of the
+ * packed 200k bed in 79 us, 2 in 84 us; one slice per block (the whole grid
+ * in one wave, reads then scatters) took 89 us */
+#ifndef DEM_IMPORT_BLOCKS
+#define DEM_IMPORT_BLOCKS 4
+#endif
+constexpr int kImportBlocksPerSM = DEM_IMPORT_BLOCKS;
+
+/* this thread's part of one slice of one array: doubles [2t, 2t+1] and
+ * [2(t+256), 2(t+256)+1] (aligned), or t, t+256, t+512 (unaligned) */
+struct SliceRegs {
+  double2 a, b;
+};
+
+__device__ __forceinline__ void slice_fetch(const double3* __restrict__ h, int n, long long slice, bool al,
+                                            SliceRegs& r) {
+  const long long i0 = slice * kImportThreads;
+  const int nd = 3 * (int)min((long long)kImportThreads, n - i0);
   const double* src = reinterpret_cast<const double*>(h + i0);
-  const int nd = 3 * cnt;
-  if ((reinterpret_cast<size_t>(src) & 15) == 0) {
-    for (int t = threadIdx.x; 2 * t < nd; t += blockDim.x) {
-      if (2 * t + 1 < nd) {
-        const double2 v = *reinterpret_cast<const double2*>(src + 2 * t);
-        sm[2 * t] = v.x;
-        sm[2 * t + 1] = v.y;
-      } else {
-        sm[2 * t] = src[2 * t];
-      }
+  const int t = threadIdx.x;
+  if (al) {
+    const int e0 = 2 * t, e1 = 2 * (t + kImportThreads);
+    r.a = e0 + 1 < nd ? *reinterpret_cast<const double2*>(src + e0)
+                      : make_double2(e0 < nd ? src[e0] : 0.0, 0.0);
+    r.b = e1 + 1 < nd ? *reinterpret_cast<const double2*>(src + e1)
+                      : make_double2(e1 < nd ? src[e1] : 0.0, 0.0);
+  } else {
+    r.a.x = t < nd ? src[t] : 0.0;
+    r.a.y = t + kImportThreads < nd ? src[t + kImportThreads] : 0.0;
+    r.b.x = t + 2 * kImportThreads < nd ? src[t + 2 * kImportThreads] : 0.0;
+    r.b.y = 0.0;
+  }
+}
+
+__device__ __forceinline__ void slice_put(const SliceRegs& r, bool al, double* sm) {
+  const int t = threadIdx.x;
+  if (al) {
+    const int e0 = 2 * t, e1 = 2 * (t + kImportThreads);
+    sm[e0] = r.a.x;
+    sm[e0 + 1] = r.a.y;
+    if (e1 < kSliceDoubles) {
+      sm[e1] = r.b.x;
+      sm[e1 + 1] = r.b.y;
     }
   } else {
-    for (int t = threadIdx.x; t < nd; t += blockDim.x) sm[t] = src[t];
+    sm[t] = r.a.x;
+    sm[t + kImportThreads] = r.a.y;
+    sm[t + 2 * kImportThreads] = r.b.x;
   }
 }
 
@@ -1357,34 +1393,56 @@ __global__ void __launch_bounds__(kImportThreads) k_import_shadows_mapped(
     const double3* __restrict__ hw, double3* __restrict__ pos, double3* __restrict__ vel, double3* __restrict__ angv,
     const double* __restrict__ rad, int* __restrict__ lqd, double3 off, int bin_exp, float lo_scale,
     float4* __restrict__ phi, float4* __restrict__ plo, float4* __restrict__ v4, float4* __restrict__ w4) {
-  __shared__ double sp[3 * kImportThreads], sv[3 * kImportThreads], sw[3 * kImportThreads];
-  stage_slice(hp, n, sp);
-  if (hv) stage_slice(hv, n, sv);
-  if (hw) stage_slice(hw, n, sw);
-  __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int t3 = 3 * threadIdx.x;
-  const int q = inv[i];
-  const double3 p = make_double3(sp[t3], sp[t3 + 1], sp[t3 + 2]);
-  const double3 v = hv ? make_double3(sv[t3], sv[t3 + 1], sv[t3 + 2]) : make_double3(0.0, 0.0, 0.0);
-  const double3 w = hw ? make_double3(sw[t3], sw[t3 + 1], sw[t3 + 2]) : make_double3(0.0, 0.0, 0.0);
-  pos[q] = p;
-  vel[q] = v;
-  angv[q] = w;
-  const int lq = __float_as_int(v4[q].w);
-  lqd[q] = lq;
-  float4 ph, pl;
-  split_hi_lo(p.x + off.x, bin_exp, lo_scale, ph.x, pl.x);
-  split_hi_lo(p.y + off.y, bin_exp, lo_scale, ph.y, pl.y);
-  split_hi_lo(p.z + off.z, bin_exp, lo_scale, ph.z, pl.z);
-  const double r = rad[q];
-  ph.w = (float)r;
-  pl.w = (float)(r - (double)ph.w);
-  phi[q] = ph;
-  plo[q] = pl;
-  v4[q] = make_float4(d2f(v.x), d2f(v.y), d2f(v.z), __int_as_float(lq));
-  w4[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
+  __shared__ double sp[kSliceDoubles], sv[kSliceDoubles], sw[kSliceDoubles];
+  const long long nsl = ((long long)n + kImportThreads - 1) / kImportThreads;
+  const bool ap = (reinterpret_cast<size_t>(hp) & 15) == 0;
+  const bool av = hv && (reinterpret_cast<size_t>(hv) & 15) == 0;
+  const bool aw = hw && (reinterpret_cast<size_t>(hw) & 15) == 0;
+  SliceRegs rp{}, rv{}, rw{};
+  long long slice = blockIdx.x;
+  if (slice < nsl) {
+    slice_fetch(hp, n, slice, ap, rp);
+    if (hv) slice_fetch(hv, n, slice, av, rv);
+    if (hw) slice_fetch(hw, n, slice, aw, rw);
+  }
+  for (; slice < nsl; slice += gridDim.x) {
+    slice_put(rp, ap, sp);
+    if (hv) slice_put(rv, av, sv);
+    if (hw) slice_put(rw, aw, sw);
+    __syncthreads();
+    const long long next = slice + gridDim.x;
+    if (next < nsl) {
+      slice_fetch(hp, n, next, ap, rp);
+      if (hv) slice_fetch(hv, n, next, av, rv);
+      if (hw) slice_fetch(hw, n, next, aw, rw);
+    }
+    const long long ii = slice * kImportThreads + threadIdx.x;
+    if (ii < n) {
+      const int i = (int)ii;
+      const int t3 = 3 * threadIdx.x;
+      const int q = inv[i];
+      const double3 p = make_double3(sp[t3], sp[t3 + 1], sp[t3 + 2]);
+      const double3 v = hv ? make_double3(sv[t3], sv[t3 + 1], sv[t3 + 2]) : make_double3(0.0, 0.0, 0.0);
+      const double3 w = hw ? make_double3(sw[t3], sw[t3 + 1], sw[t3 + 2]) : make_double3(0.0, 0.0, 0.0);
+      pos[q] = p;
+      vel[q] = v;
+      angv[q] = w;
+      const int lq = __float_as_int(v4[q].w);
+      lqd[q] = lq;
+      float4 ph, pl;
+      split_hi_lo(p.x + off.x, bin_exp, lo_scale, ph.x, pl.x);
+      split_hi_lo(p.y + off.y, bin_exp, lo_scale, ph.y, pl.y);
+      split_hi_lo(p.z + off.z, bin_exp, lo_scale, ph.z, pl.z);
+      const double r = rad[q];
+      ph.w = (float)r;
+      pl.w = (float)(r - (double)ph.w);
+      phi[q] = ph;
+      plo[q] = pl;
+      v4[q] = make_float4(d2f(v.x), d2f(v.y), d2f(v.z), __int_as_float(lq));
+      w4[q] = make_float4(d2f(w.x), d2f(w.y), d2f(w.z), 0.f);
+    }
+    __syncthreads();
+  }
 }
 
 __global__ void k_force_out(int n, const float4* __restrict__ f, double3* __restrict__ force, double3* __restrict__ mom) {
@@ -1778,9 +1836,18 @@ dem_status mixed_import_mapped(dem_ctx* c, int which, const int* inv, const doub
                                const double3* hw, cudaStream_t s) {
   MixedState* m = c->mx;
   EngineBufs& b = c->b;
-  k_import_shadows_mapped<<<grid_for(c->n, kImportThreads), kImportThreads, 0, s>>>(c->n, inv, hp, hv, hw, b.pos, b.vel, b.angv, b.rad,
-                                                               b.lqd, m->off, m->bin_exp, m->lo_scale, m->phi[which],
-                                                               m->plo[which], m->vel[which], m->angv[which]);
+  /* a few resident blocks per SM, each walking several slices */
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+  }
+  const long long nsl = ((long long)c->n + kImportThreads - 1) / kImportThreads;
+  const int grid = (int)std::min<long long>(nsl, (long long)kImportBlocksPerSM * sms);
+  k_import_shadows_mapped<<<grid, kImportThreads, 0, s>>>(c->n, inv, hp, hv, hw, b.pos, b.vel, b.angv, b.rad, b.lqd,
+                                                         m->off, m->bin_exp, m->lo_scale, m->phi[which],
+                                                         m->plo[which], m->vel[which], m->angv[which]);
   return cuda_check(cudaGetLastError(), "mixed_import_mapped launch");
 }
 
