@@ -5,8 +5,8 @@
   - the reference-compatible entry points driven in main.cpp's order (the
     first step builds the lists): sorted hashes and indices, CellStart /
     CellEnd and every neighbour slot bit-exact against the oracle
-    (kernel.cu:617-855), forces, state and histories to 1e-12, for a few steps
-    in lockstep;
+    (kernel.cu:617-855), forces, state and histories to 1e-12 (FP64 mode) or
+    within the mixed tolerances (mixed mode), for a few steps in lockstep;
   - the native engine in both precisions after 20 steps from the bed, a
     rebuild forced by re-importing its own state, then steps in lockstep with
     the oracle (tests/_lockstep.py): lists bit-exact after the rebuild, FP64 to
@@ -42,7 +42,16 @@ def bed():
     return configs.load_bed(BED)
 
 
-def test_drop_in_entry_points_at_200k_match_the_oracle(cuda, bed):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_drop_in_entry_points_at_200k_match_the_oracle(cuda, bed, precision):
+    """the reference's entry points in main.cpp's order, in either mode of
+    PpInterCalc / CirPWCalc / UpdateSystem (dem_compat_set_precision): the
+    list build bit-exact in both, the step to 1e-12 (FP64, from the bed at
+    rest) or within the mixed tolerances with at most 1 % of stage or bridge
+    labels flipped (mixed, from the bed after 20 steps of the mixed engine, as
+    the engine's own mixed lockstep starts: at exact rest every contact sits
+    on its loading turning point, where FP32 and FP64 pick the load stage
+    differently for many contacts at once)"""
     import torch
 
     from test_gpu_compat import FP64_TOL as COMPAT_TOL
@@ -50,29 +59,43 @@ def test_drop_in_entry_points_at_200k_match_the_oracle(cuda, bed):
 
     w = bed
     n = w.setup.n
-    _declare(_abi.load())
-    pos = w.pos0_reduced
-    zero = np.zeros_like(pos)
-    drv = RefDriver(w, pos, zero, zero, torch)
-    sim = _harness.OracleSim(w.setup, pos)
-    g = lambda x: x.detach().cpu().numpy()  # noqa: E731
-    for t in range(3):
-        torch.cuda.synchronize()
-        _load_oracle_from(drv, sim)
-        rb = sim.step()
-        ra = drv.step()
-        torch.cuda.synchronize()
-        assert ra == bool(rb), f"rebuild decision differs at step {t}"
-        if t == 0:
-            assert rb
-            assert np.array_equal(g(drv.hash), sim.arr("hash", np.int32, n))
-            assert np.array_equal(g(drv.index), sim.arr("index", np.int32, n))
-            assert np.array_equal(g(drv.cs), sim.arr("cellStart", np.int32, drv.C))
-            assert np.array_equal(g(drv.ce), sim.arr("cellEnd", np.int32, drv.C))
-        _lockstep.compare_step(_snap(drv, sim, w), sim, w, COMPAT_TOL, f"step {t}")
-    assert g(drv.num).mean() > 8.0
-    assert _abi.load().dem_compat_errors() == 0
-    sim.close()
+    lib = _abi.load()
+    _declare(lib)
+    mixed = precision == "mixed"
+    tol, budget = (MIXED_TOL, 0.01) if mixed else (COMPAT_TOL, 0.0)
+    _abi.check(lib.dem_compat_set_precision(1 if mixed else 0), "dem_compat_set_precision")
+    try:
+        pos = w.pos0_reduced
+        vel = ang = np.zeros_like(pos)
+        if mixed:
+            eng = Engine(w.setup, precision="mixed")
+            eng.set_state(pos)
+            eng.step(20)
+            st = eng.get_state()
+            eng.close()
+            pos, vel, ang = (np.ascontiguousarray(st[k]) for k in ("pos", "vel", "angvel"))
+        drv = RefDriver(w, pos, vel, ang, torch)
+        sim = _harness.OracleSim(w.setup, pos, vel, ang)
+        g = lambda x: x.detach().cpu().numpy()  # noqa: E731
+        for t in range(3):
+            torch.cuda.synchronize()
+            _load_oracle_from(drv, sim)
+            rb = sim.step()
+            ra = drv.step()
+            torch.cuda.synchronize()
+            assert ra == bool(rb), f"rebuild decision differs at step {t}"
+            if t == 0:
+                assert rb
+                assert np.array_equal(g(drv.hash), sim.arr("hash", np.int32, n))
+                assert np.array_equal(g(drv.index), sim.arr("index", np.int32, n))
+                assert np.array_equal(g(drv.cs), sim.arr("cellStart", np.int32, drv.C))
+                assert np.array_equal(g(drv.ce), sim.arr("cellEnd", np.int32, drv.C))
+            _lockstep.compare_step(_snap(drv, sim, w), sim, w, tol, f"step {t}", mismatch_budget=budget)
+        assert g(drv.num).mean() > 8.0
+        assert lib.dem_compat_errors() == 0
+        sim.close()
+    finally:
+        _abi.check(lib.dem_compat_set_precision(0), "dem_compat_set_precision")
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
