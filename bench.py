@@ -223,7 +223,7 @@ def run_dry(args):
     n, steps = w.setup.n, args.dry_steps
     out = {}
     for prec in ("mixed", "fp64"):
-        e = Engine(w.setup, precision=prec)
+        e = Engine(w.setup, precision=prec, pairs=args.pairs)
         e.set_state(w.pos0_reduced)
         e.step(16)
         e.sync()
