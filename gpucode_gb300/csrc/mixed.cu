@@ -1481,7 +1481,7 @@ Law32 make_law(const calParaPP& c, bool pp, double dmp_sq, int stage) {
  * PpInterCalc and CirPWCalc (kernel.cu:413-552, :958-1023) on the reference's
  * own layouts -- spheres in the caller's order, level/slot-major lists, FP64
  * SoA histories -- with the fused step's FP32 laws: a pair's overlap from the
- * FP64 positions as (d^2 - S^2) / (d + S) with d^2 - S^2 in FP64 (six FP64
+ * FP64 positions as (d^2 - S^2) / (d + S) with d^2 - S^2 in FP64 (eight FP64
  * operations, no FP64 square root, division or pow), the contact law and
  * the bridge in FP32, the sums in Kahan FP32 added to the FP64 force arrays.
  * The histories keep the spring and the peak overlap in FP64, as the fused
