@@ -155,6 +155,50 @@ def test_compat_mixed_step_loop_matches_oracle(cuda, make):
         _abi.check(lib.dem_compat_set_precision(0), "dem_compat_set_precision")
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_compat_moving_top_wall_lockstep(cuda, precision):
+    """CirPWCalc with a descending lid (CylinderBC.topv < 0, kernel.cu:966-969):
+    the entry point moves the top wall once per call before any sphere meets
+    it, in both modes, and the loop follows the oracle step by step while the
+    lid presses into the top layer (wall lists bit-exact, wall histories and
+    forces to the mode's tolerances)."""
+    import torch
+
+    w = _workloads.small_dry()
+    lib = _abi.load()
+    _declare(lib)
+    mixed = precision == "mixed"
+    tol, budget = (MIXED_TOL, 0.01) if mixed else (FP64_TOL, 0.0)
+    pos, vel, ang = _workloads.stirred(w)
+    s = w.setup.s
+    s.cyl.Tw = float((pos[:, 2] + w.setup.rad).max()) + 0.01
+    s.cyl.topv = -0.05 / (250 * s.prm.dt)  # 0.05 diameters over the run
+    _abi.check(lib.dem_compat_set_precision(1 if mixed else 0), "dem_compat_set_precision")
+    try:
+        drv = RefDriver(w, pos, vel, ang, torch)
+        sim = _harness.OracleSim(w.setup, pos, vel, ang)
+        rebuilds, touched = 0, 0
+        for t in range(250):
+            torch.cuda.synchronize()
+            _load_oracle_from(drv, sim)
+            rb = sim.step()
+            ra = drv.step()
+            torch.cuda.synchronize()
+            assert ra == bool(rb), f"rebuild decision differs at step {t}"
+            rebuilds += rb
+            _lockstep.compare_step(_snap(drv, sim, w), sim, w, tol, f"{precision} step {t}", mismatch_budget=budget)
+            # spheres in contact with the lid: a wall-list entry of kind 0 whose record has a stage
+            wl, nw = drv.wl, drv.nw
+            stage = drv.pw[0]["stage"].view(3, drv.n).t()
+            slot = torch.arange(3, device=wl.device).unsqueeze(0) < nw.unsqueeze(1)
+            touched = max(touched, int(((wl == 0) & slot & (stage != 0)).sum().item()))
+        assert rebuilds >= 2
+        assert touched > 0  # the lid reached the top layer
+        assert lib.dem_compat_errors() == 0
+    finally:
+        _abi.check(lib.dem_compat_set_precision(0), "dem_compat_set_precision")
+
+
 def test_first_step_forces_match_oracle_tightly(cuda):
     """One step from the same state: no chaotic growth, so FP64 forces agree to 1e-12."""
     import torch
