@@ -138,13 +138,21 @@ struct LawCfg64 {
 };
 
 /* elasto-plastic Hertz normal force + damping + tangential spring with slip
- * + rolling resistance, FP64, the reference's operand order */
+ * + rolling resistance, FP64, the reference's operand order.
+ *
+ * The reference's pow(x, 0.5) and pow(x, 2.0) are taken as sqrt(x) and x * x:
+ * the correctly rounded square root and product, which is what a correctly
+ * rounded pow returns for these exponents (the CPU oracle's glibc pow, within
+ * its 0.52-ulp bound; CUDA's pow carries up to 2 ulp).  The other exponents
+ * (1.5, 2/3, 3, 0.33) stay pow.  On GB300 the law is bound by FP64 issue,
+ * where each pow is some tens of FP64 instructions. */
 __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, double nrm, double3 u,
                                               double3 cpv, HistRec& h, double iRad, double rfrc,
                                               double dt, double3& dF, double3& dM, double& dR) {
   const calParaPP& cal = *c.cal;
-  /* pow(ijRad * nrm, 0.5) appears twice in the reference's law; one value */
-  const double sq = pow(ijRad * nrm, 0.5);
+  /* pow(ijRad * nrm, 0.5) (twice in the reference's law) and the damping's
+   * sqrt(ijRad * nrm): one value */
+  const double sq = sqrt(ijRad * nrm);
   double fN = 0.0;
   int st;
   if (nrm < h.plstDfm) st = 1;
@@ -161,19 +169,19 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
       h.plstRad = ijRad;
       h.plstDfm = 0.0;
     } else {
-      fN = cal.yforce_t * pow(ijRad, 2.0) + cal.ystiff_t * ijRad * (nrm - cal.ydsp_t * ijRad);
+      fN = cal.yforce_t * (ijRad * ijRad) + cal.ystiff_t * ijRad * (nrm - cal.ydsp_t * ijRad);
       h.plstRad = ijRad * (4.0 / 3.0 * cal.emod * sq * nrm) / fN;
-      h.plstDfm = nrm - pow((fN / (4.0 / 3.0 * cal.emod * pow(ijRad, 0.5))), 2.0 / 3.0);
+      h.plstDfm = nrm - pow((fN / (4.0 / 3.0 * cal.emod * sqrt(ijRad))), 2.0 / 3.0);
     }
     h.nDsp_mx = nrm;
   } else {
-    fN = 4.0 / 3.0 * cal.emod * pow(h.plstRad, 0.5) * pow((nrm - h.plstDfm), 1.5);
+    fN = 4.0 / 3.0 * cal.emod * sqrt(h.plstRad) * pow((nrm - h.plstDfm), 1.5);
   }
   h.nDsp = nrm;
 
   const double vn = dot3(cpv, u);
   double fD = 0.0;
-  if (c.damp_on) fD = -2.0 * c.dmp * cal.emod * sqrt(ijRad * nrm) * vn;
+  if (c.damp_on) fD = -2.0 * c.dmp * cal.emod * sq * vn;
 
   const double3 vt = sub3(cpv, smul3(vn, u));
   const double3 old = h.dispt;
@@ -208,16 +216,19 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
 }
 
 /* capillary bridge force, kernel.cu:65-81 (the closed-form fit of Willett et
- * al. 2000 at zero contact angle, the reference's coefficients) */
+ * al. 2000 at zero contact angle, the reference's coefficients); pow(x, 0.5)
+ * and pow(x, 2.0) as sqrt(x) and x * x (contact_law64) */
 __device__ __forceinline__ double fcap64(double Splus, double ijVol, double effectR, const LIQUID& L) {
   Splus = max(L.gapmn, Splus);
-  Splus = Splus / pow(ijVol, 0.5);
+  Splus = Splus / sqrt(ijVol);
   const double lv = log(ijVol);
-  const double f1 = -0.44507 - 0.1119 * lv - 0.012101 * pow(lv, 2.0) - 0.0005 * pow(lv, 3.0);
-  const double f2 = 1.9222 - 0.0668 * lv - 0.0013375 * pow(lv, 2.0);
-  const double f3 = 1.268 + 0.198 * lv + 0.02232 * pow(lv, 2.0) + 0.0008585 * pow(lv, 3.0);
-  const double f4 = -0.010703 + 0.03345 * lv + 0.0018574 * pow(lv, 2.0);
-  return 2 * kPiRef * effectR * L.stension * exp(f1 - f2 * exp(f3 * log(Splus) + f4 * pow(log(Splus), 2.0)));
+  const double lv2 = lv * lv, lv3 = pow(lv, 3.0);
+  const double f1 = -0.44507 - 0.1119 * lv - 0.012101 * lv2 - 0.0005 * lv3;
+  const double f2 = 1.9222 - 0.0668 * lv - 0.0013375 * lv2;
+  const double f3 = 1.268 + 0.198 * lv + 0.02232 * lv2 + 0.0008585 * lv3;
+  const double f4 = -0.010703 + 0.03345 * lv + 0.0018574 * lv2;
+  const double ls = log(Splus);
+  return 2 * kPiRef * effectR * L.stension * exp(f1 - f2 * exp(f3 * ls + f4 * (ls * ls)));
 }
 
 /* warp-aggregated counter increment */
