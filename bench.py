@@ -194,8 +194,8 @@ def run_reference(args, ws, rank):
         "vs_baseline": None, "dtype": "f64", "data": DATA, "config": bed_config(w),
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} steps of the full bed after {args.warmup} warm-up steps, on the "
-                                   "host cores (FP64 oracle restating the reference kernels; the reference sources "
-                                   "are not on this host)"},
+                                   "host cores (FP64 oracle restating the reference kernels, pinned bit for bit to "
+                                   "the reference's kernels compiled for the CPU)"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -31,6 +31,19 @@ __device__ __forceinline__ double3 cross3(double3 a, double3 b) {
   return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 
+/* The reference's pow with the exponents 1.5, 3 and 5 as products of sqrt and
+ * x: each is within about one ulp of the exact power (one correctly rounded
+ * sqrt and one or two products), tighter than the 2-ulp bound of CUDA's pow and
+ * a few FP64 instructions instead of some tens -- on GB300 the FP64 laws are
+ * bound by FP64 issue.  The CPU oracle's pow is within 0.52 ulp, so the two
+ * differ in the last bits as before, well inside the 1e-12 lockstep bound. */
+__device__ __forceinline__ double pow1_5(double x) { return x * sqrt(x); }
+__device__ __forceinline__ double cube(double x) { return x * x * x; }
+__device__ __forceinline__ double pow5(double x) {
+  const double x2 = x * x;
+  return x2 * x2 * x;
+}
+
 /* This thread's particle with the blocks taken in reverse.  Particles sit in
  * level-major cell order, so the largest spheres -- the most neighbours, the
  * longest loops -- come last; the GPU starts blocks roughly in index order,
@@ -143,9 +156,10 @@ struct LawCfg64 {
  * The reference's pow(x, 0.5) and pow(x, 2.0) are taken as sqrt(x) and x * x:
  * the correctly rounded square root and product, which is what a correctly
  * rounded pow returns for these exponents (the CPU oracle's glibc pow, within
- * its 0.52-ulp bound; CUDA's pow carries up to 2 ulp).  The other exponents
- * (1.5, 2/3, 3, 0.33) stay pow.  On GB300 the law is bound by FP64 issue,
- * where each pow is some tens of FP64 instructions. */
+ * its 0.52-ulp bound; CUDA's pow carries up to 2 ulp); pow(x, 1.5) as pow1_5.
+ * The exponent 2/3 (plastic loading only) stays pow.  On
+ * GB300 the law is bound by FP64 issue, where each pow is some tens of FP64
+ * instructions. */
 __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, double nrm, double3 u,
                                               double3 cpv, HistRec& h, double iRad, double rfrc,
                                               double dt, double3& dF, double3& dM, double& dR) {
@@ -175,7 +189,7 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
     }
     h.nDsp_mx = nrm;
   } else {
-    fN = 4.0 / 3.0 * cal.emod * sqrt(h.plstRad) * pow((nrm - h.plstDfm), 1.5);
+    fN = 4.0 / 3.0 * cal.emod * sqrt(h.plstRad) * pow1_5(nrm - h.plstDfm);
   }
   h.nDsp = nrm;
 
@@ -195,7 +209,7 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
                       (16.0 * (1 - cal.pois) * cal.emod / (4.0 - 2.0 * cal.pois) * sq);
   double ratio = 1.0;
   if (len3(dT) < dsmx) {
-    if (dsmx > c.dsmx_eps) ratio = 1.0 - pow((1.0 - len3(dT) / dsmx), 1.5);
+    if (dsmx > c.dsmx_eps) ratio = 1.0 - pow1_5(1.0 - len3(dT) / dsmx);
   } else {
     ratio = 1.0;
     if (len3(dT) > c.dsmx_eps) dT = div3(smul3(dsmx, dT), len3(dT));
@@ -216,13 +230,13 @@ __device__ __forceinline__ void contact_law64(const LawCfg64& c, double ijRad, d
 }
 
 /* capillary bridge force, kernel.cu:65-81 (the closed-form fit of Willett et
- * al. 2000 at zero contact angle, the reference's coefficients); pow(x, 0.5)
- * and pow(x, 2.0) as sqrt(x) and x * x (contact_law64) */
+ * al. 2000 at zero contact angle, the reference's coefficients); pow(x, 0.5),
+ * pow(x, 2.0) and pow(x, 3.0) as sqrt(x), x * x and cube(x) (contact_law64) */
 __device__ __forceinline__ double fcap64(double Splus, double ijVol, double effectR, const LIQUID& L) {
   Splus = max(L.gapmn, Splus);
   Splus = Splus / sqrt(ijVol);
   const double lv = log(ijVol);
-  const double lv2 = lv * lv, lv3 = pow(lv, 3.0);
+  const double lv2 = lv * lv, lv3 = cube(lv);
   const double f1 = -0.44507 - 0.1119 * lv - 0.012101 * lv2 - 0.0005 * lv3;
   const double f2 = 1.9222 - 0.0668 * lv - 0.0013375 * lv2;
   const double f3 = 1.268 + 0.198 * lv + 0.02232 * lv2 + 0.0008585 * lv3;

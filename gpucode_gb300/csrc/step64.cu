@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(128) k_pp_force64(
   double3 F = force[i];
   double3 M = mom[i];
   double R = rmom[i];
-  F.z = F.z - pow(2.0 * ir, 3.0); /* gravity, m = (2r)^3 */
+  F.z = F.z - cube(2.0 * ir); /* gravity, m = (2r)^3 */
   int wet = lqd[i];
   const int L = plevel[i];
   const long long stride = level_npars[L];
@@ -172,7 +172,7 @@ __global__ void k_liquid_share(const double* __restrict__ rad, const int* __rest
   if (i >= n) return;
   int nl = lqd_old[i];
   if (nl < 12) nl = 12;
-  pvol[i] = k.lqd.vol * pow((rad[i] * 2), 3.0) / nl;
+  pvol[i] = k.lqd.vol * cube(rad[i] * 2) / nl;
 }
 
 __global__ void k_move_top_wall(CylinderBC* cyl, double dt) {
@@ -258,7 +258,7 @@ __global__ void k_update64(const double* __restrict__ rad, double3* __restrict__
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double r = rad[i];
-  const double mass = pow(2.0 * r, 3.0);
+  const double mass = cube(2.0 * r);
   double3 v = vel[i];
   const double3 f = force[i];
   v.x = v.x + f.x * dt / mass;
@@ -268,7 +268,7 @@ __global__ void k_update64(const double* __restrict__ rad, double3* __restrict__
   pos[i] = add3(pos[i], mul3(v, dt));
   const double pm = pmove[i] + len3(v) * dt;
   pmove[i] = pm;
-  const double inert = 0.1 * pow(2.0 * r, 5.0);
+  const double inert = 0.1 * pow5(2.0 * r);
   double3 w = angvel[i];
   const double3 m = mom[i];
   w.x = w.x + m.x * dt / inert;
