@@ -32,11 +32,12 @@ __device__ __forceinline__ double3 cross3(double3 a, double3 b) {
 }
 
 /* The reference's pow with the exponents 1.5, 3 and 5 as products of sqrt and
- * x: each is within about one ulp of the exact power (one correctly rounded
- * sqrt and one or two products), tighter than the 2-ulp bound of CUDA's pow and
- * a few FP64 instructions instead of some tens -- on GB300 the FP64 laws are
- * bound by FP64 issue.  The CPU oracle's pow is within 0.52 ulp, so the two
- * differ in the last bits as before, well inside the 1e-12 lockstep bound. */
+ * x (IEEE sqrt and products, no contraction in the FP64 files): x^1.5 and x^3
+ * land within 1.3 ulp of the exact power and x^5 within 2.6 ulp (three
+ * roundings), against 2 ulp for CUDA's pow and 0.52 for the CPU oracle's --
+ * relative differences of a few 1e-16, far inside the 1e-12 lockstep bound --
+ * for a few FP64 instructions instead of some tens: on GB300 the FP64 laws are
+ * bound by FP64 issue.  pow5 only scales the integrator's spin increments. */
 __device__ __forceinline__ double pow1_5(double x) { return x * sqrt(x); }
 __device__ __forceinline__ double cube(double x) { return x * x * x; }
 __device__ __forceinline__ double pow5(double x) {
