@@ -21,7 +21,9 @@ overlap inputs):
       E* = cal.emod = E/(2(1-nu^2))  (main.cpp:330-336, kernel.cu:120);
   restitution e                      -> dmpn from a two-sphere head-on impact of
       the reference's normal law (Hertz + plastic + unload + damping) at the
-      fill's impact speed, by bisection (calibrate_dmpn);
+      fill's impact speed, by bisection (calibrate_dmpn); the same impact
+      stepped by the FP64 oracle at the dry workload's 1 us step parts at
+      0.6975 of the impact speed for e = 0.7;
   skin s                             -> CUTGAPFORNEIGHBORLIST = (s/REALSIZE)*Rmax/Rmin
       (ReadData.cpp:363 scales it back);
   bridge volume U[0.5%, 2%] of the smaller sphere -> LIQUID vol = 6 x 1.25%:
