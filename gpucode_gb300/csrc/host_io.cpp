@@ -661,8 +661,8 @@ extern "C" int ParticleFeed(FeedZone* Feedcube, CylinderBC* h_Cir, double InitPa
   };
   if (use_grid)
     for (int i = 0; i < numParticle; i++) bucket[(size_t)key(hPos[i])].push_back(i);
-  int nEach = 0, judge = 0;
-  while (judge < 500 && numParticle < NP && nEach < 60000) {
+  int nEach = 0, misses = 0;
+  while (misses < 500 && numParticle < NP && nEach < 60000) {
     double theta = 2.0 * kPi * feed_uniform();
     double u = feed_uniform() + feed_uniform();
     double mag = u > 1 ? 2 - u : u;
@@ -690,14 +690,14 @@ extern "C" int ParticleFeed(FeedZone* Feedcube, CylinderBC* h_Cir, double InitPa
       for (int i = 0; i < numParticle && !overlap; i++) overlap = test(i);
     }
     if (overlap) {
-      judge++;
+      misses++;
       continue;
     }
     hPos[numParticle] = p;
     if (use_grid) bucket[(size_t)key(p)].push_back(numParticle);
     numParticle++;
     nEach++;
-    judge = 0;
+    misses = 0;
   }
   return numParticle;
 }

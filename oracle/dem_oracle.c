@@ -350,7 +350,7 @@ static void contact_law(const law_cfg* c, double ijRad, double nrm, ov3 unitVec,
                         ov3* dF, ov3* dM, double* dR) {
   const o_calpara* cal = c->cal;
   double fN = 0.0;
-  /* load / unload / reload verdict */
+  /* load / unload / reload stage */
   int st;
   if (nrm < h.plstDfm[ine]) st = 1;
   else if (nrm >= h.plstDfm[ine] && nrm < h.nDsp[ine]) st = 3;

@@ -134,7 +134,7 @@ def test_engine_at_200k_after_a_forced_rebuild_matches_the_oracle(cuda, bed, pre
 
 
 def test_mixed_packing_metrics_at_200k_match_fp64(cuda, bed):
-    """the benchmark spec's accuracy targets on the packed bed: packing fraction
+    """the accuracy targets on the packed bed: packing fraction
     within 0.2 % and coordination number within 1 % of the FP64 run of the
     reference's formulas, after 2,000 steps from the same bed"""
     w = bed
