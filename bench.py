@@ -141,6 +141,15 @@ def slowest(local: float, ws: int, device: str = "cuda") -> float:
     return float(t.item())
 
 
+def algorithmic_bytes(n_nb: float, n_c: float, n_w: float, n_wall: float) -> float:
+    """DRAM bytes one particle-step of the fused step kernel must move, from the
+    per-particle counts of the step: the state read and written (position,
+    velocity, spin, radius: 152), 4 per neighbour-list entry, 128 per p-p
+    contact and per wall contact (the 64-byte record read and written), 16 per
+    wet non-contact bridge (flag and volume)"""
+    return 152 + 4 * n_nb + 128 * n_c + 16 * n_w + 128 * n_wall
+
+
 def replica_rate(local_s: float, particles: int, steps: int, ws: int, device: str = "cuda") -> tuple[float, float]:
     """whole-job particle-steps/s of `ws` independent replicas, each stepping
     `particles` particles `steps` times: all ranks' particle-steps over the
@@ -523,7 +532,7 @@ def run_wet_large(args, which: str):
         s1 = e.stats()
         ps = n * (steps - 16)
         cnt = {k: (s1[k] - s0[k]) / ps for k in ("nb_entries", "contacts", "bridges", "wall_contacts")}
-        bpp = 152 + 4 * cnt["nb_entries"] + 128 * cnt["contacts"] + 16 * cnt["bridges"] + 128 * cnt["wall_contacts"]
+        bpp = algorithmic_bytes(cnt["nb_entries"], cnt["contacts"], cnt["bridges"], cnt["wall_contacts"])
         ms_k = C.c_double()
         check(e.lib.dem_profile_step(e.h, 5, None, 0, C.byref(ms_k)), "dem_profile_step")
         peak, peak_kind = _peaks()
@@ -783,7 +792,7 @@ def run_headline(args, ws, rank):
     d = {k: s1[k] - s0[k] for k in ("nb_entries", "contacts", "bridges", "wall_contacts", "rebuilds")}
     ps = n * args.steps
     n_nb, n_c, n_w, n_wall = d["nb_entries"] / ps, d["contacts"] / ps, d["bridges"] / ps, d["wall_contacts"] / ps
-    bytes_per_particle = 152 + 4 * n_nb + 128 * n_c + 16 * n_w + 128 * n_wall
+    bytes_per_particle = algorithmic_bytes(n_nb, n_c, n_w, n_wall)
 
     # the fused step kernel alone, cold L2 per launch
     ms_k = C.c_double()

@@ -57,3 +57,16 @@ def test_one_rank_is_its_own_rate():
     import bench
 
     assert bench.replica_rate(0.25, 200, 4, 1) == (200 * 4 / 0.25, 0.25)
+
+
+def test_algorithmic_bytes_model():
+    """the byte model of the roofline: 152 per particle, 4 per list entry, 128
+    per contact or wall contact, 16 per bridge"""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert bench.algorithmic_bytes(0, 0, 0, 0) == 152
+    assert bench.algorithmic_bytes(8.66, 6.42, 0.84, 0.066) == pytest.approx(
+        152 + 4 * 8.66 + 128 * 6.42 + 16 * 0.84 + 128 * 0.066)
+    # the packed bed's counts give the ~1030 bytes per particle-step quoted for it
+    assert 1020 < bench.algorithmic_bytes(8.66, 6.42, 0.84, 0.066) < 1040
